@@ -1,0 +1,343 @@
+"""ctypes bindings of the native library (include/bgo.h).
+
+The library is built in-tree (``beguidedoff_gb300/_build/libbgo.so``) by
+``beguidedoff_gb300.build.build()``.  There is no CPU fallback: if the
+library is missing, every GPU entry point raises ``NativeLibraryMissing``.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+BGO_OK = 0
+BGO_ERR_ARG = -1
+BGO_ERR_CUDA = -2
+BGO_ERR_OOM = -3
+BGO_ERR_TIMEOUT = -4
+BGO_ERR_STATE = -5
+
+# Names of every function declared in include/bgo.h.
+EXPORTED = [
+    "bgo_version", "bgo_last_error", "bgo_device_count", "bgo_host_alloc", "bgo_host_free",
+    "bgo_genome_create", "bgo_genome_destroy", "bgo_genome_info", "bgo_engine_create",
+    "bgo_engine_destroy", "bgo_plan_create", "bgo_plan_destroy", "bgo_plan_info",
+    "bgo_scan_launch", "bgo_scan_collect", "bgo_engine_reserve", "bgo_search_genome",
+    "bgo_engine_info", "bgo_synth_genome", "bgo_probe_int_throughput", "bgo_scan_stats",
+]
+
+
+class NativeLibraryMissing(RuntimeError):
+    pass
+
+
+class BgoError(RuntimeError):
+    def __init__(self, code, where, message):
+        super().__init__(f"{where} failed ({code}): {message}")
+        self.code = code
+
+
+_LIB = None
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+_PP = ctypes.POINTER(ctypes.c_void_p)
+
+_SIGS = {
+    "bgo_version": ([], ctypes.c_int),
+    "bgo_last_error": ([ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+    "bgo_device_count": ([ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "bgo_host_alloc": ([_PP, ctypes.c_size_t], ctypes.c_int),
+    "bgo_host_free": ([_P], ctypes.c_int),
+    "bgo_genome_create": ([_P, _I64, _I64, _P, _I64, ctypes.c_int, _P, _PP], ctypes.c_int),
+    "bgo_genome_destroy": ([_P], ctypes.c_int),
+    "bgo_genome_info": ([_P, ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_int),
+                         ctypes.POINTER(_I64)], ctypes.c_int),
+    "bgo_engine_create": ([ctypes.c_int, _PP], ctypes.c_int),
+    "bgo_engine_destroy": ([_P], ctypes.c_int),
+    "bgo_plan_create": ([_P, _P, _P, _P, _P, _I32, _P, _PP], ctypes.c_int),
+    "bgo_plan_destroy": ([_P], ctypes.c_int),
+    "bgo_plan_info": ([_P, ctypes.POINTER(_I32), ctypes.POINTER(_I32)], ctypes.c_int),
+    "bgo_scan_launch": ([_P, _P, _P, _P, _I32, _I32, _I32, _P], ctypes.c_int),
+    "bgo_scan_collect": ([_P, _P, _I64, ctypes.POINTER(_I64), _P], ctypes.c_int),
+    "bgo_scan_stats": ([_P, ctypes.POINTER(_I64), _P], ctypes.c_int),
+    "bgo_engine_reserve": ([_P, _I64], ctypes.c_int),
+    "bgo_search_genome": ([_P, _P, _P, _P, _P, _P, _I32, _I32, _I32, _I64, _P, _P, _P, _P],
+                          ctypes.c_int),
+    "bgo_engine_info": ([_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)], ctypes.c_int),
+    "bgo_synth_genome": ([ctypes.c_uint64, _P, _I32, _P, _P, _I64, _P, ctypes.c_int, _P, _P, _P],
+                         ctypes.c_int),
+    "bgo_probe_int_throughput": ([ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
+                                 ctypes.c_int),
+}
+
+
+def synth_genome(seed, chrom_lengths, n_blocks=(), thresholds=(64, 128, 192), device=0,
+                 out=None):
+    """Seeded synthetic genome dict in the reference .npz layout (device
+    generator).  ``n_blocks`` = sorted disjoint (start, end) pairs; ``out`` may
+    supply preallocated (fwd, rc, n_mask) host arrays, e.g. pinned buffers."""
+    lens = np.ascontiguousarray(chrom_lengths, dtype=np.int64)
+    total = int(lens.sum())
+    nb = np.asarray(list(n_blocks), dtype=np.int64).reshape(-1, 2)
+    starts = np.ascontiguousarray(nb[:, 0])
+    ends = np.ascontiguousarray(nb[:, 1])
+    th = np.ascontiguousarray(thresholds, dtype=np.uint8)
+    n_words = (total + 15) // 16
+    n_bytes = (total + 7) // 8
+    if out is None:
+        fwd = np.empty(n_words, dtype=np.uint32)
+        rc = np.empty(n_words, dtype=np.uint32)
+        nm = np.empty(n_bytes, dtype=np.uint8)
+    else:
+        fwd, rc, nm = out
+        assert fwd.size >= n_words and rc.size >= n_words and nm.size >= n_bytes
+    check(lib().bgo_synth_genome(int(seed), ptr(lens), lens.size, ptr(starts), ptr(ends),
+                                 starts.size, ptr(th), int(device), fwd.ctypes.data,
+                                 rc.ctypes.data, nm.ctypes.data), "bgo_synth_genome")
+    offsets = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64)
+    return {
+        "genome_forward": fwd[:n_words], "genome_rc": rc[:n_words],
+        "chrom_names": np.array([f"chr{i + 1}" for i in range(lens.size)]),
+        "chrom_offsets": offsets, "chrom_lengths": lens, "total_bp": total,
+        "n_mask": nm[:n_bytes],
+    }
+
+
+def probe_int_throughput(op, device=0):
+    """Measured Gop/s of LOP3 (op 0), POPC (1) or 32-bit add (2)."""
+    v = ctypes.c_double()
+    check(lib().bgo_probe_int_throughput(int(device), int(op), ctypes.byref(v)),
+          "bgo_probe_int_throughput")
+    return v.value
+
+
+def library_path():
+    return _build.LIB_PATH
+
+
+def lib():
+    """The loaded library; raises NativeLibraryMissing when it was not built."""
+    global _LIB
+    if _LIB is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise NativeLibraryMissing(
+                f"native library {path} is not built; run "
+                "`python -c 'import beguidedoff_gb300.build as b; b.build()'` (needs nvcc)")
+        L = ctypes.CDLL(path)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _LIB = L
+    return _LIB
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(4096)
+    lib().bgo_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc, where):
+    if rc != BGO_OK:
+        raise BgoError(rc, where, last_error())
+
+
+def ptr(a):
+    """Address of a contiguous numpy array (None for an empty one)."""
+    if a is None or a.size == 0:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+def device_count():
+    n = ctypes.c_int(0)
+    check(lib().bgo_device_count(ctypes.byref(n)), "bgo_device_count")
+    return n.value
+
+
+class HostBuffer:
+    """Page-locked host memory viewed as a numpy array."""
+
+    def __init__(self, shape, dtype):
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * dtype.itemsize
+        p = ctypes.c_void_p()
+        check(lib().bgo_host_alloc(ctypes.byref(p), max(n, 1)), "bgo_host_alloc")
+        self._p = p
+        buf = (ctypes.c_char * max(n, 1)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def close(self):
+        if self._p is not None and self._p.value:
+            self.array = None
+            lib().bgo_host_free(self._p)
+        self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Strand:
+    """One strand array resident on the device (H/L/N bit planes)."""
+
+    def __init__(self, packed, total_bp, n_mask_le=None, device=0, stream=None):
+        packed = np.ascontiguousarray(packed, dtype=np.uint32)
+        nm = None if n_mask_le is None else np.ascontiguousarray(n_mask_le, dtype=np.uint8)
+        h = ctypes.c_void_p()
+        check(lib().bgo_genome_create(ptr(packed), packed.size, int(total_bp), ptr(nm),
+                                      0 if nm is None else nm.size, int(device), stream,
+                                      ctypes.byref(h)), "bgo_genome_create")
+        self.handle = h
+        self.total_bp = int(total_bp)
+        self.device = int(device)
+
+    def info(self):
+        tb, hn, nb = ctypes.c_int64(), ctypes.c_int(), ctypes.c_int64()
+        check(lib().bgo_genome_info(self.handle, ctypes.byref(tb), ctypes.byref(hn),
+                                    ctypes.byref(nb)), "bgo_genome_info")
+        return {"total_bp": tb.value, "has_n_mask": bool(hn.value), "device_bytes": nb.value}
+
+    def close(self):
+        if self.handle is not None and self.handle.value:
+            lib().bgo_genome_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Plan:
+    """Guide rows grouped into PAM families on the device."""
+
+    def __init__(self, engine, guide_encoded, pam_masks, pam_lens, pam_3prime, stream=None):
+        self.guides = np.ascontiguousarray(guide_encoded, dtype=np.uint64)
+        n = self.guides.size
+        pm = np.zeros((n, 6), dtype=np.uint8)
+        if n:
+            src = np.asarray(pam_masks, dtype=np.uint8).reshape(n, -1)
+            pm[:, :min(6, src.shape[1])] = src[:, :6]
+        self.pam_masks = pm
+        self.pam_lens = np.ascontiguousarray(pam_lens, dtype=np.uint8)
+        self.pam_3prime = np.ascontiguousarray(pam_3prime, dtype=np.uint8)
+        h = ctypes.c_void_p()
+        check(lib().bgo_plan_create(engine.handle, ptr(self.guides), ptr(self.pam_masks),
+                                    ptr(self.pam_lens), ptr(self.pam_3prime), n, stream,
+                                    ctypes.byref(h)), "bgo_plan_create")
+        self.handle = h
+        self.n_guides = n
+
+    def info(self):
+        nf, ng = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().bgo_plan_info(self.handle, ctypes.byref(nf), ctypes.byref(ng)),
+              "bgo_plan_info")
+        return {"n_families": nf.value, "n_guides": ng.value}
+
+    def close(self):
+        if self.handle is not None and self.handle.value:
+            lib().bgo_plan_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Engine:
+    """Per-device scan workspace (hit buffer and counters)."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        check(lib().bgo_engine_create(int(device), ctypes.byref(h)), "bgo_engine_create")
+        self.handle = h
+        self.device = int(device)
+
+    def launch(self, plan, strands, n_encoded, max_mismatches, mode=1, stream=None):
+        arr = (ctypes.c_void_p * len(strands))(*[s.handle.value for s in strands])
+        ne = np.ascontiguousarray(n_encoded, dtype=np.int32)
+        check(lib().bgo_scan_launch(self.handle, plan.handle, arr, ptr(ne), len(strands),
+                                    int(max_mismatches), int(mode), stream), "bgo_scan_launch")
+
+    def collect(self, stream=None):
+        """Waits for the last launch; returns (n_hits, sorted keys or None if
+        the device buffer overflowed)."""
+        n = ctypes.c_int64()
+        check(lib().bgo_scan_collect(self.handle, None, 0, ctypes.byref(n), stream),
+              "bgo_scan_collect")
+        if n.value > self.info()["hit_capacity"]:
+            return n.value, None
+        keys = np.empty(n.value, dtype=np.uint64)
+        if n.value == 0:
+            return 0, keys
+        check(lib().bgo_scan_collect(self.handle, ptr(keys), keys.size, ctypes.byref(n), stream),
+              "bgo_scan_collect")
+        return n.value, keys
+
+    def hit_count(self, stream=None):
+        n = ctypes.c_int64()
+        check(lib().bgo_scan_collect(self.handle, None, 0, ctypes.byref(n), stream),
+              "bgo_scan_collect")
+        return n.value
+
+    def pairs_evaluated(self, stream=None):
+        """(PAM-passing position, guide) pairs counted by the last launch."""
+        n = ctypes.c_int64()
+        check(lib().bgo_scan_stats(self.handle, ctypes.byref(n), stream), "bgo_scan_stats")
+        return n.value
+
+    def reserve(self, n_hits):
+        check(lib().bgo_engine_reserve(self.handle, int(n_hits)), "bgo_engine_reserve")
+
+    def scan(self, plan, strands, n_encoded, max_mismatches, mode=1, stream=None):
+        """Launch + collect, growing the hit buffer and re-running on overflow."""
+        self.launch(plan, strands, n_encoded, max_mismatches, mode, stream)
+        n, keys = self.collect(stream)
+        if keys is None:
+            self.reserve(n)
+            self.launch(plan, strands, n_encoded, max_mismatches, mode, stream)
+            n, keys = self.collect(stream)
+            if keys is None:
+                raise BgoError(BGO_ERR_STATE, "scan", "hit buffer overflow after reserve")
+        return keys
+
+    def info(self):
+        cap, nl = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().bgo_engine_info(self.handle, ctypes.byref(cap), ctypes.byref(nl)),
+              "bgo_engine_info")
+        return {"hit_capacity": cap.value, "launches": nl.value}
+
+    def launch_count(self):
+        return self.info()["launches"]
+
+    def close(self):
+        if self.handle is not None and self.handle.value:
+            lib().bgo_engine_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def split_keys(keys):
+    """(row, strand_slot, position, mismatches) int64 arrays from hit keys."""
+    keys = np.asarray(keys, dtype=np.uint64)
+    return ((keys >> np.uint64(39)).astype(np.int64),
+            ((keys >> np.uint64(38)) & np.uint64(1)).astype(np.int64),
+            ((keys >> np.uint64(6)) & np.uint64(0xFFFFFFFF)).astype(np.int64),
+            (keys & np.uint64(63)).astype(np.int64))

@@ -1,0 +1,124 @@
+// Internal declarations shared by the bgo translation units.
+//
+// Device genome layout (one strand array): three bit planes, 32 positions per
+// uint32 word, bit j of word w = position 32*w + j:
+//   H  - high bit of the 2-bit base (A0 C1 G2 T3 -> 0 0 1 1)
+//   L  - low bit of the 2-bit base  (            -> 0 1 0 1)
+//   N  - 1 where the N mask marks the position
+// Each plane holds `plane_words` words, zero beyond total_bp, padded so that a
+// tile load of kTileWords words starting at any tile never leaves the buffer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/bgo.h"
+
+namespace bgo {
+
+constexpr int kMaxPam = BGO_MAX_PAM_LEN;
+constexpr int kGuideLen = BGO_GUIDE_LEN;
+// The reference scans positions [0, total_bp - 26) for every PAM length
+// (beguidedoff/cuda_search.py:211).
+constexpr int kSiteSpan = 26;
+
+// Tile geometry of the scan kernels: one thread per 32-position word.
+constexpr int kTileThreads = 256;
+constexpr int kTileSites = kTileThreads * 32;     // 8192 positions
+constexpr int kTileWords = kTileSites / 32 + 4;   // + halo for window and PAM
+
+struct FamilyDesc {
+    uint8_t allowed[kMaxPam];  // IUPAC allowed-set nibble per PAM position
+    uint8_t plen;              // 1..6
+    uint8_t three_prime;       // 1: PAM after the guide
+    int32_t gbeg, gend;        // rows [gbeg, gend) of the family-sorted guide table
+};
+
+struct GuideRec {
+    uint32_t h;    // bit i = high bit of guide base i (20 bits)
+    uint32_t l;    // bit i = low bit of guide base i
+    uint32_t row;  // row index in the caller's guide table
+    uint32_t pad;
+};
+
+struct StrandDesc {
+    const uint32_t *H, *L, *N;
+    int64_t total_bp;
+    int64_t n_tiles;
+    int32_t has_n;
+    int32_t n_encoded;
+    int32_t slot;
+    int32_t pad;
+};
+
+struct ScanParams {
+    StrandDesc strand[2];
+    int32_t n_strands;
+    int32_t fam_begin, fam_end;
+    int32_t max_mm;
+    const FamilyDesc *fams;
+    const GuideRec *guides;
+    uint64_t *keys;
+    int64_t cap;
+    unsigned long long *counter;
+    int64_t tiles_total;
+};
+
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define BGO_CUDA(call)                                              \
+    do {                                                            \
+        cudaError_t _e = (call);                                    \
+        if (_e != cudaSuccess) return ::bgo::cuda_fail(_e, #call);  \
+    } while (0)
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Number of tiles covering the scanned positions [0, total_bp - 26).
+inline int64_t tiles_for(int64_t total_bp) {
+    int64_t valid = total_bp - kSiteSpan;
+    return valid > 0 ? ceil_div(valid, kTileSites) : 0;
+}
+
+// Plane words needed so every tile load [t*256, t*256 + kTileWords) is inside.
+inline int64_t plane_words_for(int64_t total_bp) {
+    int64_t t = tiles_for(total_bp);
+    int64_t need = t * (kTileSites / 32) + kTileWords;
+    int64_t cover = ceil_div(total_bp > 0 ? total_bp : 1, 32) + 4;
+    int64_t w = need > cover ? need : cover;
+    return (w + 63) / 64 * 64;
+}
+
+}  // namespace bgo
+
+struct bgo_genome {
+    int device;
+    int64_t total_bp;
+    int32_t has_n;
+    int64_t plane_words;
+    uint32_t *d_planes;  // [3][plane_words]
+    int64_t bytes;
+};
+
+struct bgo_plan {
+    int device;
+    int32_t n_guides;        // rows given by the caller
+    int32_t n_active;        // rows that can match (PAM length 1..6)
+    int32_t n_families;
+    bgo::FamilyDesc *d_fams;
+    bgo::GuideRec *d_guides;
+    bgo::FamilyDesc *h_fams;  // host copy (n_families)
+};
+
+struct bgo_engine {
+    int device;
+    uint64_t *d_keys;
+    int64_t cap;
+    unsigned long long *d_counter;
+    int64_t launches;
+    int launched;
+    int sm_count;
+};

@@ -1,0 +1,544 @@
+// Extensive off-target scan on sm_103a: plans, engine, scan kernel, collect,
+// and the search_genome_cuda drop-in.
+//
+// Semantics follow beguidedoff/cuda_search.py:163-314 (search_chunk_kernel):
+//   * positions [0, total_bp - 26) of one strand array, for every PAM length;
+//   * PAM test on the raw 2-bit bases (N encodes as A / T there), per IUPAC
+//     allowed-set nibble (equivalent to the reference's packed XOR/AND test and
+//     its per-base fallback for S/W/B/D/H/V);
+//   * raw mismatches = popcount over the 20 guide positions of
+//     (genome_high ^ guide_high) | (genome_low ^ guide_low), i.e. the
+//     reference's (x | x >> 1) & 0x5555555555 on 2-bit pairs, rejected above
+//     max_mismatches;
+//   * if any N lies in [pos, pos + 26), add the guide-window N positions whose
+//     guide base equals n_encoded, and reject again;
+//   * every surviving (row, position) is a hit with the corrected count.
+//
+// Kernel structure (one CTA = 256 threads = 8192 positions per tile):
+//   1. stage the tile's H/L/N words (+ halo) in shared memory;
+//   2. per PAM family: each thread tests its 32 positions bit-parallel
+//      (funnel shifts + LOP3), the CTA compacts the PAM-passing positions
+//      into a shared list (warp scans);
+//   3. each thread takes compacted positions and runs the family's guides
+//      (staged in shared memory, broadcast reads): 2 LOP3 + POPC per pair;
+//   4. hits are appended with one atomicAdd per warp (coalesced groups).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bgo_internal.cuh"
+
+namespace bgo {
+
+constexpr int kGuideChunk = 512;
+
+__device__ __forceinline__ uint32_t fshr(uint32_t lo, uint32_t hi, uint32_t s) {
+    return __funnelshift_r(lo, hi, s);
+}
+
+// Bit j set iff the base given by (h_j, l_j) is in IUPAC allowed-set `a`.
+__device__ __forceinline__ uint32_t allowed_bits(uint32_t h, uint32_t l, uint32_t a) {
+    uint32_t r = 0;
+    if (a & 1u) r |= ~h & ~l;
+    if (a & 2u) r |= ~h & l;
+    if (a & 4u) r |= h & ~l;
+    if (a & 8u) r |= h & l;
+    return r;
+}
+
+// Appends `key`; the lanes executing this call together share one atomicAdd.
+__device__ __forceinline__ void emit_key(uint64_t key, uint64_t *keys, int64_t cap,
+                                         unsigned long long *counter) {
+    unsigned act = __activemask();
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(act) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(act));
+    base = __shfl_sync(act, base, leader);
+    unsigned long long slot = base + (unsigned long long)__popc(act & ((1u << lane) - 1u));
+    if (slot < (unsigned long long)cap) keys[slot] = key;
+}
+
+__global__ void __launch_bounds__(kTileThreads) scan_kernel(ScanParams p) {
+    __shared__ uint32_t sH[kTileWords], sL[kTileWords], sN[kTileWords];
+    __shared__ uint16_t sList[kTileSites];
+    __shared__ uint4 sG[kGuideChunk];
+    __shared__ int sWarp[kTileThreads / 32];
+    __shared__ int sTotal;
+
+    const int t = threadIdx.x;
+    const int lane = t & 31;
+    const int warp = t >> 5;
+    const int K = p.max_mm;
+
+    for (int64_t tile = blockIdx.x; tile < p.tiles_total; tile += gridDim.x) {
+        const bool second = p.n_strands > 1 && tile >= p.strand[0].n_tiles;
+        const int64_t lt = second ? tile - p.strand[0].n_tiles : tile;
+        const uint32_t *H = second ? p.strand[1].H : p.strand[0].H;
+        const uint32_t *L = second ? p.strand[1].L : p.strand[0].L;
+        const uint32_t *N = second ? p.strand[1].N : p.strand[0].N;
+        const int64_t total_bp = second ? p.strand[1].total_bp : p.strand[0].total_bp;
+        const int has_n = second ? p.strand[1].has_n : p.strand[0].has_n;
+        const uint32_t ne = (uint32_t)(second ? p.strand[1].n_encoded : p.strand[0].n_encoded);
+        const uint64_t slot = (uint64_t)(second ? p.strand[1].slot : p.strand[0].slot);
+        const int64_t base = lt * kTileSites;
+        const int64_t w0 = lt * (kTileSites / 32);
+        const int64_t valid_end = total_bp - kSiteSpan;
+
+        __syncthreads();  // the previous tile is done with shared memory
+        for (int i = t; i < kTileWords; i += kTileThreads) {
+            sH[i] = H[w0 + i];
+            sL[i] = L[w0 + i];
+            sN[i] = N[w0 + i];
+        }
+        __syncthreads();
+
+        uint32_t valid = 0xFFFFFFFFu;
+        {
+            int64_t s0 = base + 32 * t;
+            if (s0 >= valid_end) valid = 0;
+            else if (valid_end - s0 < 32) valid = (1u << (uint32_t)(valid_end - s0)) - 1u;
+        }
+
+        for (int f = p.fam_begin; f < p.fam_end; ++f) {
+            const FamilyDesc F = p.fams[f];
+            const uint32_t pam_off = F.three_prime ? 20u : 0u;
+            const uint32_t win_off = F.three_prime ? 0u : (uint32_t)F.plen;
+
+            // (2) PAM test of this thread's 32 positions, then compaction.
+            uint32_t pass = valid;
+            for (int k = 0; k < F.plen; ++k) {
+                const uint32_t a = F.allowed[k] & 15u;
+                if (a == 15u) continue;
+                const uint32_t s = pam_off + (uint32_t)k;
+                pass &= allowed_bits(fshr(sH[t], sH[t + 1], s), fshr(sL[t], sL[t + 1], s), a);
+            }
+            const int cnt = __popc(pass);
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (lane == 31) sWarp[warp] = incl;
+            __syncthreads();
+            if (warp == 0) {
+                int v = lane < kTileThreads / 32 ? sWarp[lane] : 0;
+                int inc = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    int u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+                    if (lane >= o) inc += u;
+                }
+                if (lane < kTileThreads / 32) sWarp[lane] = inc - v;
+                if (lane == kTileThreads / 32 - 1) sTotal = inc;
+            }
+            __syncthreads();
+            {
+                int off = sWarp[warp] + incl - cnt;
+                uint32_t m = pass;
+                while (m) {
+                    int j = __ffs(m) - 1;
+                    m &= m - 1u;
+                    sList[off++] = (uint16_t)(32 * t + j);
+                }
+            }
+            __syncthreads();
+            const int n_sites = sTotal;
+            if (t == 0 && n_sites)
+                atomicAdd(p.counter + 1, (unsigned long long)n_sites * (unsigned)(F.gend - F.gbeg));
+
+            // (3) compare every compacted position with the family's guides.
+            for (int gc = F.gbeg; gc < F.gend; gc += kGuideChunk) {
+                const int gn = min(kGuideChunk, F.gend - gc);
+                for (int i = t; i < gn; i += kTileThreads) {
+                    const GuideRec r = p.guides[gc + i];
+                    sG[i] = make_uint4(r.h, r.l, r.row, 0u);
+                }
+                __syncthreads();
+                for (int idx = t; idx < n_sites; idx += kTileThreads) {
+                    const uint32_t s = sList[idx];
+                    const uint32_t wo = s + win_off;
+                    const uint32_t wi = wo >> 5, b = wo & 31u;
+                    const uint32_t h20 = fshr(sH[wi], sH[wi + 1], b) & 0xFFFFFu;
+                    const uint32_t l20 = fshr(sL[wi], sL[wi + 1], b) & 0xFFFFFu;
+#pragma unroll 4
+                    for (int g = 0; g < gn; ++g) {
+                        const uint4 G = sG[g];
+                        const int c = __popc((h20 ^ G.x) | (l20 ^ G.y));
+                        if (c <= K) {
+                            int mmf = c;
+                            if (has_n) {
+                                const uint32_t n26 =
+                                    fshr(sN[s >> 5], sN[(s >> 5) + 1], s & 31u) & 0x3FFFFFFu;
+                                if (n26) {
+                                    const uint32_t n20 = fshr(sN[wi], sN[wi + 1], b) & 0xFFFFFu;
+                                    const uint32_t eh = (ne & 2u) ? G.x : ~G.x;
+                                    const uint32_t el = (ne & 1u) ? G.y : ~G.y;
+                                    mmf = c + __popc(n20 & eh & el);
+                                }
+                            }
+                            if (mmf <= K) {
+                                const uint64_t pos = (uint64_t)(base + s);
+                                const uint64_t key = ((uint64_t)G.z << 39) | (slot << 38) |
+                                                     (pos << 6) | (uint64_t)mmf;
+                                emit_key(key, p.keys, p.cap, p.counter);
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+    }
+}
+
+static int blocks_per_sm() {
+    static int cached = 0;
+    if (!cached) {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, scan_kernel, kTileThreads, 0) !=
+                cudaSuccess ||
+            n <= 0)
+            n = 1;
+        cached = n;
+    }
+    return cached;
+}
+
+}  // namespace bgo
+
+using namespace bgo;
+
+// ----------------------------------------------------------------------------
+// engine
+// ----------------------------------------------------------------------------
+extern "C" int bgo_engine_create(int device, bgo_engine **out) {
+    if (!out) return BGO_ERR_ARG;
+    *out = nullptr;
+    BGO_CUDA(cudaSetDevice(device));
+    bgo_engine *e = new (std::nothrow) bgo_engine();
+    if (!e) return BGO_ERR_OOM;
+    e->device = device;
+    e->cap = 0;
+    cudaError_t ce = cudaMalloc(&e->d_counter, 2 * sizeof(unsigned long long));
+    if (ce == cudaSuccess) ce = cudaMemset(e->d_counter, 0, 2 * sizeof(unsigned long long));
+    int sms = 0;
+    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (ce != cudaSuccess) {
+        if (e->d_counter) cudaFree(e->d_counter);
+        delete e;
+        return cuda_fail(ce, "bgo_engine_create");
+    }
+    e->sm_count = sms;
+    *out = e;
+    return bgo_engine_reserve(e, 1 << 20);
+}
+
+extern "C" int bgo_engine_destroy(bgo_engine *e) {
+    if (!e) return BGO_OK;
+    cudaSetDevice(e->device);
+    if (e->d_keys) cudaFree(e->d_keys);
+    if (e->d_counter) cudaFree(e->d_counter);
+    delete e;
+    return BGO_OK;
+}
+
+extern "C" int bgo_engine_reserve(bgo_engine *e, int64_t n_hits) {
+    if (!e || n_hits < 0) return BGO_ERR_ARG;
+    if (n_hits <= e->cap) return BGO_OK;
+    BGO_CUDA(cudaSetDevice(e->device));
+    int64_t cap = std::max<int64_t>(n_hits, e->cap * 2);
+    uint64_t *p = nullptr;
+    BGO_CUDA(cudaMalloc(&p, (size_t)cap * sizeof(uint64_t)));
+    if (e->d_keys) cudaFree(e->d_keys);
+    e->d_keys = p;
+    e->cap = cap;
+    return BGO_OK;
+}
+
+extern "C" int bgo_engine_info(const bgo_engine *e, int64_t *hit_capacity, int64_t *n_launches) {
+    if (!e) return BGO_ERR_ARG;
+    if (hit_capacity) *hit_capacity = e->cap;
+    if (n_launches) *n_launches = e->launches;
+    return BGO_OK;
+}
+
+// ----------------------------------------------------------------------------
+// plan
+// ----------------------------------------------------------------------------
+extern "C" int bgo_plan_create(bgo_engine *engine, const uint64_t *guide_encoded,
+                               const uint8_t *pam_masks, const uint8_t *pam_lens,
+                               const uint8_t *pam_3prime, int32_t n_guides, void *stream,
+                               bgo_plan **out) {
+    if (!engine || !out || n_guides < 0 ||
+        (n_guides > 0 && (!guide_encoded || !pam_masks || !pam_lens || !pam_3prime))) {
+        set_error("bgo_plan_create: invalid argument");
+        return BGO_ERR_ARG;
+    }
+    if (n_guides >= (1 << 25)) {
+        set_error("bgo_plan_create: at most 2^25 - 1 guide rows");
+        return BGO_ERR_ARG;
+    }
+    *out = nullptr;
+    BGO_CUDA(cudaSetDevice(engine->device));
+    // Group rows by (allowed nibbles, length, orientation), first-seen order.
+    std::map<std::vector<uint8_t>, int> fam_index;
+    std::vector<std::vector<int32_t>> members;
+    std::vector<FamilyDesc> fams;
+    for (int32_t i = 0; i < n_guides; ++i) {
+        const int plen = pam_lens[i];
+        if (plen <= 0 || plen > kMaxPam) continue;  // never matches (cuda_search.py:139-140)
+        std::vector<uint8_t> key(kMaxPam + 2, 0);
+        for (int k = 0; k < plen; ++k) key[k] = pam_masks[i * kMaxPam + k] & 15u;
+        key[kMaxPam] = (uint8_t)plen;
+        key[kMaxPam + 1] = pam_3prime[i] ? 1 : 0;
+        auto it = fam_index.find(key);
+        int f;
+        if (it == fam_index.end()) {
+            f = (int)fams.size();
+            fam_index.emplace(key, f);
+            FamilyDesc d{};
+            for (int k = 0; k < kMaxPam; ++k) d.allowed[k] = key[k];
+            d.plen = (uint8_t)plen;
+            d.three_prime = key[kMaxPam + 1];
+            fams.push_back(d);
+            members.emplace_back();
+        } else {
+            f = it->second;
+        }
+        members[f].push_back(i);
+    }
+    std::vector<GuideRec> recs;
+    recs.reserve(n_guides);
+    for (size_t f = 0; f < fams.size(); ++f) {
+        fams[f].gbeg = (int32_t)recs.size();
+        for (int32_t i : members[f]) {
+            GuideRec r{};
+            const uint64_t v = guide_encoded[i];
+            for (int k = 0; k < kGuideLen; ++k) {
+                const uint32_t b = (uint32_t)((v >> (2 * k)) & 3u);
+                r.h |= ((b >> 1) & 1u) << k;
+                r.l |= (b & 1u) << k;
+            }
+            r.row = (uint32_t)i;
+            recs.push_back(r);
+        }
+        fams[f].gend = (int32_t)recs.size();
+    }
+    bgo_plan *pl = new (std::nothrow) bgo_plan();
+    if (!pl) return BGO_ERR_OOM;
+    pl->device = engine->device;
+    pl->n_guides = n_guides;
+    pl->n_active = (int32_t)recs.size();
+    pl->n_families = (int32_t)fams.size();
+    pl->h_fams = new (std::nothrow) FamilyDesc[fams.size() + 1];
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = pl->h_fams ? cudaSuccess : cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) {
+        std::copy(fams.begin(), fams.end(), pl->h_fams);
+        e = cudaMalloc(&pl->d_fams, sizeof(FamilyDesc) * (fams.size() + 1));
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&pl->d_guides, sizeof(GuideRec) * (recs.size() + 1));
+    if (e == cudaSuccess && !fams.empty())
+        e = cudaMemcpyAsync(pl->d_fams, fams.data(), sizeof(FamilyDesc) * fams.size(),
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && !recs.empty())
+        e = cudaMemcpyAsync(pl->d_guides, recs.data(), sizeof(GuideRec) * recs.size(),
+                            cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        bgo_plan_destroy(pl);
+        return cuda_fail(e, "bgo_plan_create");
+    }
+    *out = pl;
+    return BGO_OK;
+}
+
+extern "C" int bgo_plan_destroy(bgo_plan *pl) {
+    if (!pl) return BGO_OK;
+    cudaSetDevice(pl->device);
+    if (pl->d_fams) cudaFree(pl->d_fams);
+    if (pl->d_guides) cudaFree(pl->d_guides);
+    delete[] pl->h_fams;
+    delete pl;
+    return BGO_OK;
+}
+
+extern "C" int bgo_plan_info(const bgo_plan *pl, int32_t *n_families, int32_t *n_guides) {
+    if (!pl) return BGO_ERR_ARG;
+    if (n_families) *n_families = pl->n_families;
+    if (n_guides) *n_guides = pl->n_guides;
+    return BGO_OK;
+}
+
+// ----------------------------------------------------------------------------
+// scan
+// ----------------------------------------------------------------------------
+static void fill_strand(StrandDesc &d, const bgo_genome *g, int32_t n_encoded, int32_t slot) {
+    d.H = g->d_planes;
+    d.L = g->d_planes + g->plane_words;
+    d.N = g->d_planes + 2 * g->plane_words;
+    d.total_bp = g->total_bp;
+    d.n_tiles = tiles_for(g->total_bp);
+    d.has_n = g->has_n;
+    d.n_encoded = n_encoded;
+    d.slot = slot;
+    d.pad = 0;
+}
+
+extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
+                               const bgo_genome *const *strands, const int32_t *n_encoded,
+                               int32_t n_strands, int32_t max_mismatches, int32_t mode,
+                               void *stream) {
+    if (!engine || !plan || !strands || !n_encoded || n_strands < 1 || n_strands > 2 ||
+        (mode != 0 && mode != 1)) {
+        set_error("bgo_scan_launch: invalid argument");
+        return BGO_ERR_ARG;
+    }
+    for (int i = 0; i < n_strands; ++i) {
+        if (!strands[i] || strands[i]->device != engine->device ||
+            (n_encoded[i] < 0 || n_encoded[i] > 3)) {
+            set_error("bgo_scan_launch: bad strand or n_encoded");
+            return BGO_ERR_ARG;
+        }
+    }
+    if (plan->device != engine->device) {
+        set_error("bgo_scan_launch: plan and engine on different devices");
+        return BGO_ERR_ARG;
+    }
+    BGO_CUDA(cudaSetDevice(engine->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    BGO_CUDA(cudaMemsetAsync(engine->d_counter, 0, 2 * sizeof(unsigned long long), s));
+    engine->launched = 1;
+    if (plan->n_families == 0) return BGO_OK;
+    ScanParams p{};
+    p.max_mm = max_mismatches;
+    p.fams = plan->d_fams;
+    p.guides = plan->d_guides;
+    p.keys = engine->d_keys;
+    p.cap = engine->cap;
+    p.counter = engine->d_counter;
+    const int64_t max_grid = (int64_t)engine->sm_count * blocks_per_sm();
+    if (mode == 0) {
+        for (int i = 0; i < n_strands; ++i) {
+            fill_strand(p.strand[0], strands[i], n_encoded[i], i);
+            p.n_strands = 1;
+            p.tiles_total = p.strand[0].n_tiles;
+            if (p.tiles_total == 0) continue;
+            const int64_t grid = std::min<int64_t>(p.tiles_total, max_grid);
+            for (int f = 0; f < plan->n_families; ++f) {
+                p.fam_begin = f;
+                p.fam_end = f + 1;
+                scan_kernel<<<(unsigned)grid, kTileThreads, 0, s>>>(p);
+                BGO_CUDA(cudaGetLastError());
+                engine->launches++;
+            }
+        }
+    } else {
+        for (int i = 0; i < n_strands; ++i) fill_strand(p.strand[i], strands[i], n_encoded[i], i);
+        p.n_strands = n_strands;
+        p.tiles_total = p.strand[0].n_tiles + (n_strands > 1 ? p.strand[1].n_tiles : 0);
+        if (p.tiles_total == 0) return BGO_OK;
+        p.fam_begin = 0;
+        p.fam_end = plan->n_families;
+        const int64_t grid = std::min<int64_t>(p.tiles_total, max_grid);
+        scan_kernel<<<(unsigned)grid, kTileThreads, 0, s>>>(p);
+        BGO_CUDA(cudaGetLastError());
+        engine->launches++;
+    }
+    return BGO_OK;
+}
+
+extern "C" int bgo_scan_collect(bgo_engine *engine, uint64_t *keys, int64_t capacity,
+                                int64_t *n_hits, void *stream) {
+    if (!engine || !n_hits || capacity < 0) return BGO_ERR_ARG;
+    if (!engine->launched) {
+        set_error("bgo_scan_collect: no launch to collect");
+        return BGO_ERR_STATE;
+    }
+    BGO_CUDA(cudaSetDevice(engine->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long n = 0;
+    BGO_CUDA(cudaMemcpyAsync(&n, engine->d_counter, sizeof(n), cudaMemcpyDeviceToHost, s));
+    BGO_CUDA(cudaStreamSynchronize(s));
+    *n_hits = (int64_t)n;
+    if (keys && (int64_t)n <= capacity && (int64_t)n <= engine->cap && n > 0) {
+        BGO_CUDA(cudaMemcpyAsync(keys, engine->d_keys, (size_t)n * sizeof(uint64_t),
+                                 cudaMemcpyDeviceToHost, s));
+        BGO_CUDA(cudaStreamSynchronize(s));
+        std::sort(keys, keys + n);
+    }
+    return BGO_OK;
+}
+
+extern "C" int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream) {
+    if (!engine || !pairs_evaluated) return BGO_ERR_ARG;
+    if (!engine->launched) {
+        set_error("bgo_scan_stats: no launch");
+        return BGO_ERR_STATE;
+    }
+    BGO_CUDA(cudaSetDevice(engine->device));
+    unsigned long long v = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    BGO_CUDA(cudaMemcpyAsync(&v, engine->d_counter + 1, sizeof(v), cudaMemcpyDeviceToHost, s));
+    BGO_CUDA(cudaStreamSynchronize(s));
+    *pairs_evaluated = (int64_t)v;
+    return BGO_OK;
+}
+
+// ----------------------------------------------------------------------------
+// search_genome_cuda drop-in
+// ----------------------------------------------------------------------------
+extern "C" int bgo_search_genome(bgo_engine *engine, const bgo_genome *strand,
+                                 const uint64_t *guide_encoded, const uint8_t *pam_masks,
+                                 const uint8_t *pam_lens, const uint8_t *pam_3prime,
+                                 int32_t n_guides, int32_t max_mismatches, int32_t n_encoded,
+                                 int64_t results_per_guide, int64_t *hit_counts,
+                                 int64_t *hit_positions, int8_t *hit_mismatches, void *stream) {
+    if (!engine || !strand || n_guides < 0 || results_per_guide < 0 ||
+        (n_guides > 0 && !hit_counts) ||
+        (results_per_guide > 0 && n_guides > 0 && (!hit_positions || !hit_mismatches))) {
+        set_error("bgo_search_genome: invalid argument");
+        return BGO_ERR_ARG;
+    }
+    bgo_plan *plan = nullptr;
+    int rc = bgo_plan_create(engine, guide_encoded, pam_masks, pam_lens, pam_3prime, n_guides,
+                             stream, &plan);
+    if (rc != BGO_OK) return rc;
+    std::vector<uint64_t> keys;
+    int64_t n = 0;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        rc = bgo_scan_launch(engine, plan, &strand, &n_encoded, 1, max_mismatches, 0, stream);
+        if (rc == BGO_OK) rc = bgo_scan_collect(engine, nullptr, 0, &n, stream);
+        if (rc != BGO_OK) break;
+        if (n <= engine->cap) break;
+        rc = bgo_engine_reserve(engine, n);
+        if (rc != BGO_OK) break;
+    }
+    if (rc == BGO_OK) {
+        try {
+            keys.resize((size_t)n);
+        } catch (...) {
+            rc = BGO_ERR_OOM;
+        }
+    }
+    if (rc == BGO_OK && n > 0) rc = bgo_scan_collect(engine, keys.data(), n, &n, stream);
+    bgo_plan_destroy(plan);
+    if (rc != BGO_OK) return rc;
+    for (int32_t g = 0; g < n_guides; ++g) hit_counts[g] = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        const uint64_t k = keys[(size_t)i];
+        const int64_t g = (int64_t)(k >> 39);
+        const int64_t c = hit_counts[g]++;
+        if (c < results_per_guide) {
+            hit_positions[g * results_per_guide + c] = (int64_t)((k >> 6) & 0xFFFFFFFFull);
+            hit_mismatches[g * results_per_guide + c] = (int8_t)(k & 63u);
+        }
+    }
+    return BGO_OK;
+}

@@ -1,0 +1,391 @@
+"""Extensive-mode finder: the drop-in for beguidedoff/finder.py:256-679.
+
+Same constructor, ``search()`` signature, output columns, row order, sorting,
+error types and log messages as the reference.  The genome strands stay on the
+GPU (``bgo_genome_create``); one device scan covers every scan key and both
+strands (``bgo_scan_launch``), and the exact hit keys come back sorted.  All
+host post-processing is vectorised NumPy over the hit arrays instead of the
+reference's per-hit Python loops.
+
+Reference behaviours kept on purpose (each pinned by tests/golden):
+  * strand '-' positions map through the reverse-complement array per
+    chromosome (finder.py:43-62); windows straddling chromosome junctions are
+    reported as the reference reports them, including a chromosome index of -1
+    (Python's last element) for negative leftmost positions;
+  * on-target exclusion on (chromosome index, local leftmost, strand)
+    (finder.py:208-218); ``ot_sequence`` / ``ot_pam`` decoded from the scanned
+    strand array, so an N reads as A on '+' and T on '-' (:221-234);
+  * mismatch positions from guide vs decoded window, so N-corrected positions
+    are counted in ``n_mismatches`` but not listed (:435-437);
+  * ``include_non_editable`` is ignored; ``return_all`` decides (:508);
+  * per-strand hit limits of the re-scan escalation (:568-638): a scan key
+    whose hits on a strand exceed ``max_results_per_guide`` keeps that many
+    (here: the genome-order prefix) and a warning gives the exact count.
+"""
+import logging
+from collections import defaultdict
+from pathlib import Path
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+from . import _native
+from .base_editing import TARGET_2BIT
+from .encoding import encode_dna, encode_guide_64bit, extract_windows
+from .genome_converter import load_genome
+from .io import load_guides_from_tsv
+from .pam import encode_pam_mask
+from .scoring import cctop_from_masks
+from .table import COLUMNS, Table, concat, pandas_available
+from .types import GuideInput
+
+_LOGGER = logging.getLogger("beguidedoff")
+
+_DEFAULT_RESULTS_PER_GUIDE = 10240
+_MAX_RESULTS_PER_GUIDE = 2_621_440
+_DECODE = np.array(list("ACGT"))
+_PROFILES = str(Path(__file__).resolve().parent / "base_editor_profiles.tsv")
+
+
+def _device_index(device) -> int:
+    if device is None:
+        try:
+            n = _native.device_count()
+        except _native.NativeLibraryMissing:
+            raise
+        if n == 0:
+            raise RuntimeError("Extensive mode requires a CUDA GPU (no CUDA device is visible). "
+                               "Use the fast CPU mode instead: "
+                               "`beguidedoff(mode='fast', index_path=...)`.")
+        return 0
+    spec = str(device)
+    if not spec.startswith("cuda"):
+        raise RuntimeError(f"Extensive mode requires a CUDA GPU (device '{spec}'). "
+                           "Use the fast CPU mode instead: "
+                           "`beguidedoff(mode='fast', index_path=...)`.")
+    return int(spec.split(":")[1]) if ":" in spec else 0
+
+
+def prepare_n_masks(genome: dict) -> Tuple[Optional[np.ndarray], Optional[np.ndarray]]:
+    """Little-bit-order N masks for the forward and reverse-complement arrays
+    (finder.py:310-345), padded by 16 bytes; (None, None) without any N."""
+    packed_big = genome.get("n_mask")
+    total_bp = int(genome["total_bp"])
+    if packed_big is None or np.asarray(packed_big).size == 0:
+        return None, None
+    bits = np.unpackbits(np.asarray(packed_big, dtype=np.uint8), bitorder="big", count=total_bp)
+    if not bits.any():
+        return None, None
+    fwd = np.pad(np.packbits(bits, bitorder="little"), (0, 16))
+    rc_bits = np.empty_like(bits)
+    for off, ln in zip(np.asarray(genome["chrom_offsets"]), np.asarray(genome["chrom_lengths"])):
+        off, ln = int(off), int(ln)
+        rc_bits[off:off + ln] = bits[off:off + ln][::-1]
+    rc = np.pad(np.packbits(rc_bits, bitorder="little"), (0, 16))
+    return fwd, rc
+
+
+class beguidedoff:
+    """GPU brute-force off-target search (extensive mode)."""
+
+    def __init__(self, genome_path: str, max_mismatches: int = 4, scoring_method: str = "CCTOP",
+                 device: Optional[str] = None, n_top_offtargets: int = 3,
+                 results_per_guide: int = 10240, max_results_per_guide: Optional[int] = None,
+                 genome_data: Optional[dict] = None, scan_mode: int = 1):
+        self.genome_path = genome_path
+        self.max_mismatches = max_mismatches
+        if scoring_method.upper() != "CCTOP":
+            raise ValueError("extensive mode only supports scoring_method='CCTOP'")
+        self.scoring_method = "CCTOP"
+        self.n_top_offtargets = n_top_offtargets
+        self.results_per_guide = results_per_guide
+        self.max_results_per_guide = max_results_per_guide
+        self.scan_mode = scan_mode
+        self.device_index = _device_index(device)
+        self.device = f"cuda:{self.device_index}"
+        self._init_host(genome_data if genome_data is not None else load_genome(genome_path))
+        self._engine = _native.Engine(self.device_index)
+        masks = [self._n_mask_fwd, self._n_mask_rc][:len(self._strand_arrays)]
+        self._strands = [_native.Strand(a, self.total_bp, m, self.device_index)
+                         for a, m in zip(self._strand_arrays, masks)]
+
+    def _init_host(self, genome_data: dict) -> None:
+        """Host-side genome tables (no device state)."""
+        self.genome_data = g = genome_data
+        self.total_bp = int(g["total_bp"])
+        self.chrom_names = [str(c) for c in g["chrom_names"]]
+        self.chrom_offsets = np.asarray(g["chrom_offsets"], dtype=np.int64)
+        self.chrom_lengths = np.asarray(g["chrom_lengths"], dtype=np.int64)
+        self._n_mask_fwd, self._n_mask_rc = prepare_n_masks(g)
+        self._strand_arrays = [np.ascontiguousarray(g["genome_forward"], dtype=np.uint32)]
+        if "genome_rc" in g:
+            self._strand_arrays.append(np.ascontiguousarray(g["genome_rc"], dtype=np.uint32))
+        order = np.argsort(np.array(self.chrom_names, dtype=object), kind="stable")
+        self._chrom_rank = np.empty(len(order), dtype=np.int64)
+        self._chrom_rank[order] = np.arange(len(order))
+
+    @classmethod
+    def host_only(cls, genome_data: dict, max_mismatches: int = 4, n_top_offtargets: int = 3,
+                  results_per_guide: int = 10240, max_results_per_guide: Optional[int] = None):
+        """A finder without device state whose ``search_with_keys`` assembles
+        the output from externally supplied hit keys (used to test the host
+        post-processing without a GPU)."""
+        self = cls.__new__(cls)
+        self.genome_path = None
+        self.max_mismatches = max_mismatches
+        self.scoring_method = "CCTOP"
+        self.n_top_offtargets = n_top_offtargets
+        self.results_per_guide = results_per_guide
+        self.max_results_per_guide = max_results_per_guide
+        self.scan_mode = 1
+        self.device_index, self.device = -1, "none"
+        self._engine, self._strands = None, []
+        self._init_host(genome_data)
+        return self
+
+    @property
+    def genome_info(self) -> dict:
+        return {"build": "unknown", "total_bp": self.total_bp,
+                "n_chromosomes": len(self.chrom_names), "chromosomes": self.chrom_names}
+
+    def close(self):
+        for s in getattr(self, "_strands", []):
+            s.close()
+        self._strands = []
+        if getattr(self, "_engine", None) is not None:
+            self._engine.close()
+            self._engine = None
+
+    # ------------------------------------------------------------------
+    def _deduplicate_guides(self, guides: List[GuideInput]):
+        """Scan keys (seq, pam, on-target chrom index, local leftmost, strand)
+        in first-seen order and the input rows of each (finder.py:361-403)."""
+        mapping: Dict[tuple, List[GuideInput]] = defaultdict(list)
+        for g in guides:
+            ci = lp = st = None
+            if g.on_target_chrom and g.on_target_pos is not None:
+                ci = next((i for i, n in enumerate(self.chrom_names)
+                           if n == g.on_target_chrom), None)
+                if ci is not None:
+                    if g.on_target_strand is None:
+                        raise ValueError(
+                            f"Guide {g.guide_id} has on-target chromosome and position but no "
+                            f"strand. Please provide on_target_strand ('+' or '-').")
+                    window = 20 + len(g.pam)
+                    lp = g.on_target_pos - 1 if g.on_target_strand == "+" else \
+                        g.on_target_pos - window
+                    st = g.on_target_strand
+            mapping[(g.guide_seq, g.pam, ci, lp, st)].append(g)
+        return list(mapping), mapping
+
+    def _scan(self, plan_seqs: List[str], plan_pams: List[str]) -> np.ndarray:
+        """Device scan of both strands; sorted hit keys."""
+        n = len(plan_seqs)
+        gv = np.array([encode_guide_64bit(encode_dna(s)[:20]) for s in plan_seqs],
+                      dtype=np.uint64)
+        pm = np.zeros((n, 6), dtype=np.uint8)
+        for i, pam in enumerate(plan_pams):
+            pm[i] = encode_pam_mask(pam)
+        pl = np.array([len(p) for p in plan_pams], dtype=np.uint8)
+        p3 = np.ones(n, dtype=np.uint8)
+        plan = _native.Plan(self._engine, gv, pm, pl, p3)
+        try:
+            ne = [0, 3][:len(self._strands)]
+            return self._engine.scan(plan, self._strands, ne, self.max_mismatches,
+                                     mode=self.scan_mode)
+        finally:
+            plan.close()
+
+    def _limits(self, counts2: np.ndarray, keys, log) -> np.ndarray:
+        """Per scan key the per-strand number of hits kept, with the warnings
+        of the reference's overflow re-scan loop (finder.py:568-638)."""
+        cap = (self.max_results_per_guide if self.max_results_per_guide is not None
+               else _MAX_RESULTS_PER_GUIDE)
+        mx = counts2.max(axis=1) if counts2.size else np.zeros(0, dtype=np.int64)
+        limit = np.full(len(keys), self.results_per_guide, dtype=np.int64)
+        pending = np.nonzero(mx > self.results_per_guide)[0]
+        rpg = self.results_per_guide
+        while pending.size:
+            if rpg >= cap:
+                for i in sorted(pending.tolist(), key=lambda j: keys[j][0]):
+                    log.warning(
+                        "Truncated off-target enumeration for guide %s (PAM=%s): %d raw "
+                        "genome-wide hits exceed the per-strand buffer of %d; keeping the "
+                        "first %d (genome order). The off-target count for this guide is a "
+                        "lower bound.", keys[i][0], keys[i][1], int(counts2[i].sum()), rpg,
+                        int(np.minimum(counts2[i], rpg).sum()))
+                break
+            rpg = min(rpg * 16, cap)
+            if log is not None:
+                names = ", ".join(sorted({keys[i][0] for i in pending.tolist()})[:5])
+                log.warning("Hit buffer overflow for %d guide(s) at results_per_guide=%s "
+                            "(e.g. %s); re-scanning them with results_per_guide=%d.",
+                            pending.size, self.results_per_guide, names, rpg)
+            limit[pending] = rpg
+            pending = pending[mx[pending] > rpg]
+        return limit
+
+    # ------------------------------------------------------------------
+    def search(self, input_file: Optional[str] = None, guides: Optional[List[GuideInput]] = None,
+               return_all: bool = False, count_score_threshold: Optional[float] = None,
+               output_file: Optional[str] = None, include_non_editable: bool = False,
+               presets_path: Optional[str] = None, verbose: bool = True,
+               logger: Optional[logging.Logger] = None):
+        if (input_file is None) == (guides is None):
+            raise ValueError("Exactly one of input_file or guides must be provided")
+        if input_file is not None:
+            guides = load_guides_from_tsv(input_file, presets_path=presets_path or _PROFILES)
+        if not guides:
+            raise ValueError("No guides provided")
+        log = logger if logger is not None else _LOGGER
+        for g in guides:
+            if g.pam_position.lower() != "3prime":
+                raise ValueError(f"Guide {g.guide_id} has pam_position '{g.pam_position}'. "
+                                 f"Only 3prime PAM is supported.")
+        keys, mapping = self._deduplicate_guides(guides)
+        if verbose:
+            log.info("Guides after deduplication: %d (from %d input rows)", len(keys),
+                     len(guides))
+            log.info("Running GPU search on %s ...", self.device)
+        # one plan row per distinct (seq, pam); scan keys that differ only in
+        # their on-target share it
+        plan_index: Dict[tuple, int] = {}
+        key_plan = np.empty(len(keys), dtype=np.int64)
+        for i, k in enumerate(keys):
+            key_plan[i] = plan_index.setdefault((k[0], k[1]), len(plan_index))
+        plan_items = list(plan_index)
+        hit_keys = self._scan([s for s, _ in plan_items], [p for _, p in plan_items])
+        table = self._assemble(hit_keys, keys, key_plan, plan_items, mapping, guides, return_all,
+                               count_score_threshold, log)
+        if output_file:
+            table.to_csv(output_file, sep="\t", index=False)
+            if verbose:
+                log.info("Wrote results to %s", output_file)
+        return table
+
+    # ------------------------------------------------------------------
+    def _assemble(self, hit_keys, keys, key_plan, plan_items, mapping, guides, return_all,
+                  count_score_threshold, log):
+        row, slot, pos, mm = _native.split_keys(hit_keys)
+        n_plan = len(plan_items)
+        counts2 = np.zeros((n_plan, 2), dtype=np.int64)
+        np.add.at(counts2, (row, slot), 1)
+        limit = self._limits(counts2[key_plan], keys, log)
+        offsets, lengths = self.chrom_offsets, self.chrom_lengths
+        # keys are sorted by (row, strand, position): ranges per row, and the
+        # rank of each hit inside its (row, strand) group
+        r_lo = np.searchsorted(row, np.arange(n_plan), side="left")
+        r_hi = np.searchsorted(row, np.arange(n_plan), side="right")
+        grp = row * 2 + slot
+        rank = np.arange(grp.size) - np.searchsorted(grp, grp, side="left")
+        plen_plan = np.array([len(p) for _, p in plan_items], dtype=np.int64)
+        # decode windows and PAMs from the scanned strand arrays
+        seq = np.zeros((grp.size, 20), dtype=np.uint8)
+        pam = np.zeros((grp.size, 6), dtype=np.uint8)
+        for s in range(len(self._strand_arrays)):
+            sel = np.nonzero(slot == s)[0]
+            if sel.size:
+                arr = self._strand_arrays[s]
+                seq[sel] = extract_windows(arr, pos[sel], 20)
+                pam[sel] = extract_windows(arr, pos[sel] + 20, 6)
+        plen = plen_plan[row]
+        window = 20 + plen
+        leftmost = pos.copy()
+        minus = slot == 1
+        if minus.any():
+            ci = np.searchsorted(offsets, pos[minus], side="right") - 1
+            local_rc = pos[minus] - offsets[ci]
+            leftmost[minus] = offsets[ci] + (lengths[ci] - local_rc - window[minus])
+        report = np.where(minus, leftmost + window - 1, pos)
+        rep_ci = np.searchsorted(offsets, report, side="right") - 1
+        rep_local = report - offsets[rep_ci]
+        # leftmost as (chromosome index, local) for the on-target test; a
+        # negative leftmost gives index -1, which never equals an on-target
+        ot_ci_hit = np.searchsorted(offsets, leftmost, side="right") - 1
+        ot_local_hit = leftmost - offsets[ot_ci_hit]
+        # mismatch masks (guide vs decoded window) and exact CCTOP scores
+        mmask = np.zeros(grp.size, dtype=np.int64)
+        weights = np.int64(1) << np.arange(20, dtype=np.int64)
+        for p_i in range(n_plan):
+            a, b = r_lo[p_i], r_hi[p_i]
+            if a == b:
+                continue
+            gb = np.zeros(20, dtype=np.uint8)
+            enc = encode_dna(plan_items[p_i][0])[:20]
+            gb[:enc.size] = enc
+            mmask[a:b] = ((seq[a:b] != gb[None, :]).astype(np.int64) * weights[None, :]).sum(1)
+        score = cctop_from_masks(mmask)
+        include_non_editable = return_all
+        below: Dict[str, int] = defaultdict(int)
+        per_input: Dict[str, List[np.ndarray]] = defaultdict(list)
+        for ki, key in enumerate(keys):
+            p_i = key_plan[ki]
+            sel = np.arange(r_lo[p_i], r_hi[p_i])
+            sel = sel[rank[sel] < limit[ki]]
+            if key[2] is not None and sel.size:
+                st_code = 0 if key[4] == "+" else 1
+                excl = ((ot_ci_hit[sel] == key[2]) & (ot_local_hit[sel] == key[3])
+                        & (slot[sel] == st_code))
+                sel = sel[~excl]
+            for g in mapping[key]:
+                tb = TARGET_2BIT.get(g.editor_type)
+                if tb is None:
+                    raise ValueError(f"Unknown editor_type: {g.editor_type}")
+                # positions range(start - 1, end) below 20, indexed like a str
+                cols = [i if i >= 0 else 20 + i
+                        for i in range(g.edit_window_start - 1, g.edit_window_end) if i < 20]
+                if any(c < 0 for c in cols):
+                    raise IndexError("string index out of range")
+                if cols and sel.size:
+                    editable = (seq[sel][:, cols] == tb).any(axis=1)
+                else:
+                    editable = np.zeros(sel.size, dtype=bool)
+                per_input[g.guide_id].append(sel if include_non_editable else sel[editable])
+                if count_score_threshold is not None:
+                    below[g.guide_id] += int(
+                        (editable & (score[sel] <= count_score_threshold)).sum())
+        tables = []
+        for g in guides:
+            parts = per_input.get(g.guide_id)
+            keep = np.concatenate(parts) if parts else np.zeros(0, dtype=np.int64)
+            if keep.size == 0:
+                continue
+            order = np.lexsort((slot[keep], rep_local[keep], self._chrom_rank[rep_ci[keep]],
+                                score[keep]))
+            keep = keep[order]
+            if not return_all:
+                keep = keep[:self.n_top_offtargets]
+            tables.append(self._table(keep, g, seq, pam, plen, mm, mmask, score, slot, rep_ci,
+                                      rep_local, plan_items, row, below.get(g.guide_id, 0)))
+        t = concat(tables) if tables else Table()
+        if pandas_available():
+            import pandas as pd
+
+            return t.to_pandas() if tables else pd.DataFrame()
+        return t
+
+    def _table(self, idx, g, seq, pam, plen, mm, mmask, score, slot, rep_ci, rep_local,
+               plan_items, row, n_below):
+        n = idx.size
+        seq_s = ["".join(r) for r in _DECODE[seq[idx]]]
+        pam_s = ["".join(r[:k]) for r, k in zip(_DECODE[pam[idx]], plen[idx].tolist())]
+        mpos = [",".join(str(i + 1) for i in range(20) if (m >> i) & 1)
+                for m in mmask[idx].tolist()]
+        cols = {
+            "guide_rna_sequence": np.array([plan_items[r][0] for r in row[idx].tolist()],
+                                           dtype=object),
+            "base_editor": np.array([g.base_editor or ""] * n, dtype=object),
+            "ot_rank": np.arange(1, n + 1, dtype=np.int64),
+            "ot_chromosome": np.array([self.chrom_names[c] for c in rep_ci[idx].tolist()],
+                                      dtype=object),
+            "ot_position": (rep_local[idx] + 1).astype(np.int64),
+            "ot_strand": np.where(slot[idx] == 1, "-", "+").astype(object),
+            "ot_sequence": np.array(seq_s, dtype=object),
+            "ot_pam": np.array(pam_s, dtype=object),
+            "n_mismatches": mm[idx].astype(np.int64),
+            "mismatch_positions": np.array(mpos, dtype=object),
+            "score": np.array([round(float(v), 6) for v in score[idx].tolist()],
+                              dtype=np.float64),
+            "n_offtargets_below_threshold": np.full(n, n_below, dtype=np.int64),
+        }
+        return Table(cols, COLUMNS)

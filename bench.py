@@ -1,0 +1,411 @@
+"""Benchmark of the extensive off-target scan on one node.
+
+Workload (default): the human-scale plain scan - a synthetic 3.1 Gbp genome of
+24 chromosomes (47-249 Mbp, rescaled), GC 41% i.i.d., 5% N in blocks
+(log-uniform 10 kb - 3 Mb), 100 random 20-nt guides with PAM NGG, ABE/CBE
+windows 4-8 split 50/50, max_mismatches 4, both strands.  Seeded synthetic
+data stands in for GRCh38 (not available offline).
+
+A step = one scan of both strands against all guides.  ``value`` is guide-site
+comparisons/s with the genome resident in HBM: guides x sum over strands of
+(total_bp - 26) (the reference's per-strand site count) / kernel seconds,
+timed with CUDA events on the launch stream.  ``e2e`` is the same metric
+through the public finder API with every step uploading both strand arrays
+and N masks from pinned host memory and reading the hits back.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--mode 0|1] [--genome-bp B] [--guides G]
+
+Under torchrun each rank scans the full workload on its own GPU (weak
+scaling, no data-path collective); value = all ranks' comparisons / the
+slowest rank's time.  ``--impl reference`` times the CPU restatement of the
+reference scan (oracle/) on all host cores on a bounded sample per step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "guide-site comparisons/s"
+UNIT = "cmp/s"
+
+
+def make_workload(genome_bp, n_guides, seed=2):
+    """Chromosome lengths, N blocks and guides of the human-scale config."""
+    rng = np.random.default_rng(seed)
+    n_chrom = 24
+    raw = rng.uniform(47e6, 249e6, n_chrom)
+    lens = np.floor(raw / raw.sum() * genome_bp).astype(np.int64)
+    lens[0] += genome_bp - int(lens.sum())
+    n_total = int(0.05 * genome_bp)
+    blk = []
+    while sum(blk) < n_total:
+        blk.append(int(np.exp(rng.uniform(np.log(10_000), np.log(3_000_000)))))
+    blk[-1] -= sum(blk) - n_total
+    blk = [b for b in blk if b > 0]
+    free = genome_bp - n_total
+    gaps = np.floor(rng.dirichlet(np.ones(len(blk) + 1)) * free).astype(np.int64)
+    order = rng.permutation(len(blk))
+    blocks, pos = [], 0
+    for i, bi in enumerate(order):
+        pos += int(gaps[i])
+        blocks.append((pos, pos + blk[bi]))
+        pos += blk[bi]
+    guides = ["".join(rng.choice(list("ACGT"), 20)) for _ in range(n_guides)]
+    return lens, blocks, guides
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def start(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self._proc = None
+            return self
+        threading.Thread(target=self._read, daemon=True).start()
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            if self._stop.is_set():
+                break
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        self._stop.set()
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+        return self.summary()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def dist_max(x, ws):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def plan_arrays(guides):
+    from beguidedoff_gb300.encoding import encode_dna, encode_guide_64bit
+    from beguidedoff_gb300.pam import encode_pam_mask
+
+    n = len(guides)
+    gv = np.array([encode_guide_64bit(encode_dna(g)) for g in guides], dtype=np.uint64)
+    pm = np.tile(encode_pam_mask("NGG"), (n, 1))
+    return gv, pm, np.full(n, 3, dtype=np.uint8), np.ones(n, dtype=np.uint8)
+
+
+def cpu_scan_rate(genome, guides, max_mm, target_s, n_threads=0, budget_bp=None):
+    """Oracle scan of both strands on a bounded prefix sample; returns
+    (cmp/s, threads, sample description, seconds)."""
+    from oracle import oracle as O
+
+    gv, pm, pl, p3 = plan_arrays(guides)
+    fwd_nm, rc_nm = O.prepare_n_masks(genome) if budget_bp is None else (None, None)
+    nms = (genome.get("_nm_fwd_le"), genome.get("_nm_rc_le"))
+    if nms[0] is not None:
+        fwd_nm, rc_nm = nms
+    tb = genome["total_bp"]
+
+    def run(span):
+        t0 = time.perf_counter()
+        for arr, nm, ne in ((genome["genome_forward"], fwd_nm, 0),
+                            (genome["genome_rc"], rc_nm, 3)):
+            O.scan_strand(arr, tb, nm, gv, pm, pl, p3, max_mm, ne, 0, span, n_threads)
+        return time.perf_counter() - t0
+
+    span = 2_000_000
+    dt = run(span)
+    span = int(min(tb - 26, max(span, span * target_s / max(dt, 1e-3))))
+    dt = run(span)
+    threads = n_threads or O.max_threads()
+    rate = len(guides) * 2 * span / dt
+    return rate, threads, f"positions [0, {span}) of both strands x {len(guides)} guides", dt
+
+
+def bench_reference(args, ws, rank):
+    """CPU restatement of the reference scan (no compiled reference exists for
+    this path: the reference kernel is Numba-JIT CUDA) on all host cores."""
+    if rank != 0:
+        return
+    from beguidedoff_gb300 import _native
+
+    lens, blocks, guides = make_workload(args.genome_bp, args.guides)
+    try:
+        genome = _native.synth_genome(7, lens, blocks, thresholds=(76, 128, 180),
+                                      device=int(os.environ.get("LOCAL_RANK", "0")))
+    except Exception:  # no GPU: generate nothing large on the host
+        raise
+    from beguidedoff_gb300.finder import prepare_n_masks
+
+    genome["_nm_fwd_le"], genome["_nm_rc_le"] = prepare_n_masks(genome)
+    per_step = max(1.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_scan_rate(genome, guides, args.max_mm, per_step / 4)
+    rates, sample, threads = [], "", 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, threads, sample, _dt = cpu_scan_rate(genome, guides, args.max_mm, per_step)
+        rates.append(r)
+    wall = time.perf_counter() - t0
+    value = statistics.median(rates)
+    comps = args.guides * 2 * (int(lens.sum()) - 26)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * comps / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": workload_config(args, lens),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample + " per step (oracle/scan_oracle.c, OpenMP)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+    print(json.dumps(out))
+
+
+def workload_config(args, lens):
+    return {
+        "workload": (f"human-scale plain scan: synthetic {int(lens.sum()) / 1e9:.2f} Gbp, "
+                     f"24 chromosomes, GC 41%, 5% N blocks, {args.guides} random NGG guides, "
+                     f"max_mismatches {args.max_mm}, both strands"),
+        "genome_bp": int(lens.sum()), "guides": args.guides, "pam": "NGG",
+        "max_mismatches": args.max_mm, "scan_mode": args.mode,
+        "l2": "inputs larger than L2 (bit planes of both strands ~2.3 GB)",
+    }
+
+
+def bench_ours(args, ws, rank, local):
+    import torch
+
+    from beguidedoff_gb300 import _native, build
+    from beguidedoff_gb300.finder import beguidedoff
+    from beguidedoff_gb300.types import GuideInput
+
+    build.build()
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    lens, blocks, guides = make_workload(args.genome_bp, args.guides)
+    total = int(lens.sum())
+    n_words, n_bytes = (total + 15) // 16, (total + 7) // 8
+    pin = [_native.HostBuffer((n_words,), np.uint32), _native.HostBuffer((n_words,), np.uint32),
+           _native.HostBuffer((n_bytes,), np.uint8)]
+    t0 = time.perf_counter()
+    genome = _native.synth_genome(7, lens, blocks, thresholds=(76, 128, 180), device=local,
+                                  out=[b.array for b in pin])
+    t_synth = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    f = beguidedoff(None, max_mismatches=args.max_mm, genome_data=genome,
+                    device=f"cuda:{local}", scan_mode=args.mode)
+    t_init = time.perf_counter() - t0
+    nm_pin = []
+    for m in (f._n_mask_fwd, f._n_mask_rc):
+        hb = _native.HostBuffer((m.size,), np.uint8)
+        hb.array[:] = m
+        nm_pin.append(hb)
+    gv, pm, pl, p3 = plan_arrays(guides)
+    plan = _native.Plan(f._engine, gv, pm, pl, p3)
+    eng = f._engine
+    comps = args.guides * 2 * (total - 26)
+
+    # -------- device-resident kernel timing (value) --------
+    for _ in range(args.warmup):
+        eng.launch(plan, f._strands, [0, 3], args.max_mm, args.mode, sp)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    n0 = eng.launch_count()
+    clocks = ClockSampler(local).start()
+    time.sleep(0.3)
+    barrier(ws)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for k in range(args.steps):
+        eng.launch(plan, f._strands, [0, 3], args.max_mm, args.mode, sp)
+        ev[k + 1].record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clk = clocks.stop()
+    launches = eng.launch_count() - n0
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    t_max = dist_max(total_ms / 1e3, ws)
+    hits = eng.hit_count(sp)
+    pairs = eng.pairs_evaluated(sp)
+
+    # -------- roofline: the compare loop is POPC-bound (1 POPC per pair) --------
+    popc_peak = _native.probe_int_throughput(1, local)
+    lop3_peak = _native.probe_int_throughput(0, local)
+    per_launch_s = (total_ms / 1e3) / max(1, launches)
+    pairs_per_launch = pairs / max(1, launches // args.steps) if args.mode == 0 else pairs
+    achieved = pairs / (total_ms / 1e3 / args.steps) / 1e9
+    plane_bytes = sum(3 * s.info()["device_bytes"] // 3 for s in f._strands)
+    hbm_peak = None
+    try:
+        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, KeyError, ValueError):
+        hbm_peak = 6800.0
+    hbm_achieved = plane_bytes / (total_ms / 1e3 / args.steps) / 1e9
+
+    # -------- end to end through the public API, genome uploaded each step --------
+    ginputs = [GuideInput(f"row_{i}", g, "NGG", "3prime", 4, 8, "ABE" if i % 2 == 0 else "CBE",
+                          base_editor="ABE8e" if i % 2 == 0 else "TadCBEd")
+               for i, g in enumerate(guides)]
+    for s in f._strands:
+        s.close()
+
+    def e2e_step():
+        f._strands = [_native.Strand(pin[0].array, total, nm_pin[0].array, local, sp),
+                      _native.Strand(pin[1].array, total, nm_pin[1].array, local, sp)]
+        t = f.search(guides=ginputs, verbose=False, count_score_threshold=5.0)
+        for s in f._strands:
+            s.close()
+        return t
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    n1 = eng.launch_count()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        table = e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = dist_max((time.perf_counter() - t0) / args.steps, ws)
+    e2e_launches = eng.launch_count() - n1
+    h2d = (pin[0].array.nbytes + pin[1].array.nbytes + nm_pin[0].array.nbytes
+           + nm_pin[1].array.nbytes + gv.nbytes + pm.nbytes + pl.nbytes + p3.nbytes)
+    d2h = 8 * hits + 8
+
+    # -------- CPU baseline (oracle, all host cores, bounded sample) --------
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        genome["_nm_fwd_le"], genome["_nm_rc_le"] = f._n_mask_fwd, f._n_mask_rc
+        rate, threads, sample, dt = cpu_scan_rate(genome, guides, args.max_mm, args.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": sample + f" ({dt:.1f} s, oracle/scan_oracle.c OpenMP)"}
+
+    if rank == 0:
+        value = ws * comps / (t_max / args.steps)
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic", "config": workload_config(args, lens),
+            "roofline": {
+                "bound": "int", "unit": "Gop/s", "achieved": achieved, "peak": popc_peak,
+                "frac": achieved / popc_peak, "traffic": None,
+                "op": "POPC (one per PAM-passing position x guide pair)",
+                "peak_source": "measured live: bgo_probe_int_throughput(POPC)",
+                "pairs_per_step": pairs, "lop3_peak_gops": lop3_peak,
+                "hbm": {"achieved_gbs": hbm_achieved, "peak_gbs": hbm_peak,
+                        "frac": hbm_achieved / hbm_peak, "bytes_per_step": plane_bytes},
+            },
+            "cpu_baseline": cpu,
+            "e2e": {"value": ws * comps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "s_per_step": e2e_s,
+                    "rows": len(table), "launches": e2e_launches // args.steps},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "hits_per_step": hits,
+            "step_ms": step_ms,
+            "setup_s": {"synth": t_synth, "finder_init": t_init},
+        }
+        print(json.dumps(out))
+    plan.close()
+    f.close()
+    for b in pin + nm_pin:
+        b.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--genome-bp", type=int, default=3_100_000_000)
+    ap.add_argument("--guides", type=int, default=100)
+    ap.add_argument("--max-mm", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        bench_reference(args, ws, rank)
+    else:
+        bench_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

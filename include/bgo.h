@@ -1,0 +1,176 @@
+/*
+ * bgo.h - C ABI of the GB300 (sm_103a) extensive off-target scan.
+ *
+ * Plain C types only: host pointers, sizes, and `void *stream` standing for a
+ * cudaStream_t (NULL = the legacy default stream).  Every function returns an
+ * int status (BGO_OK or a negative BGO_ERR_*); the message of the last failure
+ * on the calling thread is available from bgo_last_error().
+ *
+ * Reference interfaces replaced (paths inside ltschmitt/BEguidedOFF):
+ *   beguidedoff/cuda_search.py:384-488  search_genome_cuda(...)  -> bgo_search_genome
+ *   beguidedoff/cuda_search.py:321-381  device genome / N-mask caches
+ *                                       -> bgo_genome_create / bgo_genome_destroy
+ *   beguidedoff/cuda_search.py:124-160  encode_pam_packed (host PAM precompile)
+ *                                       -> bgo_plan_create (PAM families, guide planes)
+ *   beguidedoff/cuda_search.py:163-314  search_chunk_kernel launches
+ *                                       -> bgo_scan_launch / bgo_scan_collect
+ *
+ * Hit keys (uint64, ascending order = (guide, strand, position)):
+ *   bits  0..5   mismatches after the N correction
+ *   bits  6..37  0-based position in the scanned strand array
+ *   bit  38      strand slot (index into the genome list given to the launch)
+ *   bits 39..63  guide row index in the plan (input order)
+ */
+#ifndef BGO_H
+#define BGO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BGO_OK 0
+#define BGO_ERR_ARG (-1)      /* invalid argument                           */
+#define BGO_ERR_CUDA (-2)     /* a CUDA runtime call failed                 */
+#define BGO_ERR_OOM (-3)      /* device or host allocation failed           */
+#define BGO_ERR_TIMEOUT (-4)  /* a bounded device wait gave up              */
+#define BGO_ERR_STATE (-5)    /* call order violated (e.g. collect w/o launch) */
+
+#define BGO_MAX_PAM_LEN 6
+#define BGO_GUIDE_LEN 20
+
+#define BGO_KEY_MM(k) ((int)((k) & 63u))
+#define BGO_KEY_POS(k) ((int64_t)(((k) >> 6) & 0xFFFFFFFFull))
+#define BGO_KEY_STRAND(k) ((int)(((k) >> 38) & 1u))
+#define BGO_KEY_GUIDE(k) ((int64_t)((k) >> 39))
+
+typedef struct bgo_genome bgo_genome;
+typedef struct bgo_plan bgo_plan;
+typedef struct bgo_engine bgo_engine;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int bgo_version(void);
+
+/* Copies the last error message of this thread (NUL-terminated, truncated). */
+int bgo_last_error(char *buf, size_t len);
+
+/* Number of CUDA devices visible to the process. */
+int bgo_device_count(int *n);
+
+/* Page-locked host buffers for fast host<->device copies. */
+int bgo_host_alloc(void **ptr, size_t bytes);
+int bgo_host_free(void *ptr);
+
+/*
+ * Uploads one strand array (the reference .npz layout: 2-bit bases A0 C1 G2 T3,
+ * 16 per uint32, base i at bits 2*(i%16) of word i/16) and its N mask
+ * (little bit order, bit i = position i; NULL or 0 bytes = no N gating, as the
+ * reference does for genomes without N) to `device`, converting it to the
+ * device layout (high-bit, low-bit and N planes, 32 positions per word).
+ * Replaces the id()-keyed upload caches of beguidedoff/cuda_search.py:321-381.
+ * The host buffers are only read during the call.  total_bp < 2^32.
+ */
+int bgo_genome_create(const uint32_t *packed, int64_t n_words, int64_t total_bp,
+                      const uint8_t *n_mask_le, int64_t n_mask_bytes, int device,
+                      void *stream, bgo_genome **out);
+int bgo_genome_destroy(bgo_genome *genome);
+/* total_bp, whether an N mask is present, and the device bytes held. */
+int bgo_genome_info(const bgo_genome *genome, int64_t *total_bp, int *has_n_mask,
+                    int64_t *device_bytes);
+
+/* Engine: per-device workspace (hit buffer, counters) reused across scans.
+ * One engine serves one thread / stream at a time. */
+int bgo_engine_create(int device, bgo_engine **out);
+int bgo_engine_destroy(bgo_engine *engine);
+
+/*
+ * Guide plan: one row per scan key, in the reference's kernel-input form
+ * (beguidedoff/finder.py:167-177): guide_encoded[i] = 20 bases, 2 bits each,
+ * LSB first; pam_masks[i*6 + k] = IUPAC allowed-set nibble (bit0 A .. bit3 T)
+ * of PAM position k; pam_lens[i] in 0..6 (0 or >6 = row never matches, as
+ * encode_pam_packed leaves its length field 0); pam_3prime[i] 1 = PAM after
+ * the guide, 0 = before.  Rows are grouped into PAM families on the device.
+ */
+int bgo_plan_create(bgo_engine *engine, const uint64_t *guide_encoded, const uint8_t *pam_masks,
+                    const uint8_t *pam_lens, const uint8_t *pam_3prime, int32_t n_guides,
+                    void *stream, bgo_plan **out);
+int bgo_plan_destroy(bgo_plan *plan);
+/* Number of PAM families and rows of a plan. */
+int bgo_plan_info(const bgo_plan *plan, int32_t *n_families, int32_t *n_guides);
+
+/*
+ * Enqueues the scan of `n_strands` (1 or 2) strand arrays against every plan
+ * row on `stream`; no host synchronisation.  n_encoded[s] is the 2-bit value
+ * an N encodes as on strand s (0 forward, 3 reverse complement).  Positions
+ * scanned: [0, total_bp - 26) of each strand, as the reference kernel.
+ * mode: 0 = one kernel per PAM family and strand (plain form),
+ *       1 = one persistent launch over all families and strands.
+ */
+int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genome *const *strands,
+                    const int32_t *n_encoded, int32_t n_strands, int32_t max_mismatches,
+                    int32_t mode, void *stream);
+
+/*
+ * Waits for the last launch of `engine`, then reports the exact number of hits
+ * in *n_hits and, when keys != NULL and *n_hits <= capacity, copies all hit
+ * keys to `keys` in ascending order.  If *n_hits > capacity nothing is copied;
+ * call bgo_scan_launch again after bgo_engine_reserve(engine, *n_hits).
+ */
+int bgo_scan_collect(bgo_engine *engine, uint64_t *keys, int64_t capacity, int64_t *n_hits,
+                     void *stream);
+
+/* After the last launch completed: number of (PAM-passing position, guide
+ * row) pairs whose mismatches were counted.  No reference counterpart: it is
+ * the work figure of the roofline. */
+int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
+
+/* Grows the engine's device hit buffer to at least `n_hits` keys. */
+int bgo_engine_reserve(bgo_engine *engine, int64_t n_hits);
+
+/*
+ * Drop-in for search_genome_cuda (beguidedoff/cuda_search.py:384-488) on one
+ * strand: hit_counts[g] = exact number of matches of row g (the reference's
+ * counts dict), and rows g of hit_positions / hit_mismatches (row stride
+ * results_per_guide) hold its first min(count, results_per_guide) hits in
+ * genome order (the reference records them in atomic order).
+ */
+int bgo_search_genome(bgo_engine *engine, const bgo_genome *strand, const uint64_t *guide_encoded,
+                      const uint8_t *pam_masks, const uint8_t *pam_lens,
+                      const uint8_t *pam_3prime, int32_t n_guides, int32_t max_mismatches,
+                      int32_t n_encoded, int64_t results_per_guide, int64_t *hit_counts,
+                      int64_t *hit_positions, int8_t *hit_mismatches, void *stream);
+
+/* Reserved device hit capacity (keys) and number of kernels launched since
+ * creation (diagnostics); either pointer may be NULL. */
+int bgo_engine_info(const bgo_engine *engine, int64_t *hit_capacity, int64_t *n_launches);
+
+/*
+ * Seeded synthetic genome in the reference .npz layout (what
+ * beguidedoff/genome_converter.py:15-108 writes for the equivalent FASTA):
+ * chromosomes of the given lengths concatenated, bases drawn per position from
+ * cumulative byte thresholds (A below t[0], C below t[1], G below t[2], else T),
+ * N in the sorted disjoint half-open blocks [n_starts[i], n_ends[i]).
+ * Outputs (host): fwd_out / rc_out ceil(total/16) words, n_mask_big_out
+ * ceil(total/8) bytes in np.packbits (big) bit order.  No reference
+ * counterpart: it stands in for the real assemblies the benchmarks used.
+ */
+int bgo_synth_genome(uint64_t seed, const int64_t *chrom_lengths, int32_t n_chroms,
+                     const int64_t *n_starts, const int64_t *n_ends, int64_t n_blocks,
+                     const uint8_t *thresholds, int device, uint32_t *fwd_out, uint32_t *rc_out,
+                     uint8_t *n_mask_big_out);
+
+/*
+ * Measured throughput (Gop/s) of one integer instruction on `device`:
+ * op 0 = LOP3, 1 = POPC, 2 = 32-bit add.  Independent chains, 8 CTAs of 256
+ * threads per SM, best of 3 timed launches.  No reference counterpart: it is
+ * the roofline denominator of the scan kernels.
+ */
+int bgo_probe_int_throughput(int device, int op, double *gops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BGO_H */

@@ -36,10 +36,19 @@ class Guide:
     base_editor: Optional[str] = None
 
 
+class _Arrays(dict):
+    """Decompressed fixture arrays with the NpzFile ``files`` attribute."""
+
+    @property
+    def files(self):
+        return list(self.keys())
+
+
 class Case:
     def __init__(self, name):
         self.name = name
-        self.d = np.load(os.path.join(GOLDEN_DIR, name + ".npz"), allow_pickle=False)
+        with np.load(os.path.join(GOLDEN_DIR, name + ".npz"), allow_pickle=False) as z:
+            self.d = _Arrays({k: z[k] for k in z.files})
         self.meta = json.loads(str(self.d["meta_json"]))
 
     def genome(self):

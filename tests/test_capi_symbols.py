@@ -1,0 +1,34 @@
+"""The C-ABI library builds here, loads, and exports every function that
+include/bgo.h declares (no device calls: this runs without a GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from beguidedoff_gb300 import _native, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    txt = open(os.path.join(ROOT, "include", "bgo.h")).read()
+    return sorted(set(re.findall(r"^int (bgo_\w+)\(", txt, flags=re.M)))
+
+
+def test_header_and_binding_agree():
+    assert _declared() == sorted(_native.EXPORTED)
+
+
+def test_library_exports_every_declared_symbol():
+    try:
+        path = build.build()
+    except (RuntimeError, FileNotFoundError) as e:  # no nvcc on this host
+        pytest.skip(f"cannot build: {e}")
+    lib = ctypes.CDLL(path)
+    for name in _declared():
+        assert hasattr(lib, name), name
+    lib.bgo_version.restype = ctypes.c_int
+    assert lib.bgo_version() >= 100
+    buf = ctypes.create_string_buffer(64)
+    assert lib.bgo_last_error(buf, 64) == 0

@@ -1,0 +1,235 @@
+"""GPU parity: the sm_103a scan through the C ABI against the reference's
+recorded outputs and the C oracle (bit-exact hit sets, identical tables)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from _golden import FINDER_CASES, Case, rows_equal
+from _keys import oracle_keys, table_rows
+from beguidedoff_gb300 import _native, build
+from beguidedoff_gb300 import cuda_search as CS
+from beguidedoff_gb300.finder import beguidedoff, prepare_n_masks
+from beguidedoff_gb300.types import GuideInput
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+IUPAC = O.IUPAC_MASK
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    build.build()
+    assert _native.device_count() >= 1
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("name", FINDER_CASES)
+def test_finder_tables_match_reference(name, mode):
+    case = Case(name)
+    meta = case.meta
+    f = beguidedoff(None, max_mismatches=meta["max_mismatches"],
+                    n_top_offtargets=meta["n_top_offtargets"],
+                    results_per_guide=meta["results_per_guide"],
+                    max_results_per_guide=meta["max_results_per_guide"],
+                    genome_data=case.genome(), scan_mode=mode)
+    try:
+        for ri, run in enumerate(meta["runs"]):
+            t = f.search(guides=case.guides(GuideInput), verbose=False, **run["kwargs"])
+            ok, why = rows_equal(table_rows(t), case.expected_rows(ri))
+            assert ok, f"{name} mode {mode} run {ri}: {why}"
+    finally:
+        f.close()
+
+
+@pytest.mark.parametrize("name", FINDER_CASES)
+def test_seam_matches_reference_raw_calls(name):
+    case = Case(name)
+    g = case.genome()
+    fwd, rc = prepare_n_masks(g)
+    for i in range(case.meta["raw_calls"]):
+        c = case.raw_call(i)
+        ne = int(c["n_encoded"])
+        arr, nm = (g["genome_forward"], fwd) if ne == 0 else (g["genome_rc"], rc)
+        if len(c["guide_encoded"]) > CS.MAX_GUIDES:
+            continue
+        res, ovf, cnt = CS.search_genome_cuda(
+            arr, g["total_bp"], c["guide_encoded"], c["pam_masks"], c["pam_lens"],
+            c["pam_3prime"], int(c["max_mismatches"]), return_overflow=True,
+            results_per_guide=int(c["results_per_guide"]), n_mask_packed=nm, n_encoded=ne)
+        for gi in range(len(c["guide_encoded"])):
+            sel = c["hit_guide"] == gi
+            exp = list(zip(c["hit_pos"][sel].tolist(), c["hit_mm"][sel].tolist()))
+            assert res[gi] == exp, (name, i, gi)
+            assert cnt[gi] == int(c["counts"][gi])
+
+
+def test_seam_5prime_exotic_and_overflow_flags():
+    case = Case("seam_5prime")
+    d = case.d
+    g = case.genome()
+    fwd, rc = prepare_n_masks(g)
+    for i in range(case.meta["raw_calls"]):
+        c = case.raw_call(i)
+        minus = str(c["strand"]) == "-"
+        res, ovf, cnt = CS.search_genome_cuda(
+            g["genome_rc"] if minus else g["genome_forward"], g["total_bp"], d["guide_encoded"],
+            d["pam_masks"], d["pam_lens"], c["pam_3prime"], int(c["max_mismatches"]),
+            return_overflow=True, results_per_guide=int(c["results_per_guide"]),
+            n_mask_packed=rc if minus else fwd, n_encoded=int(c["n_encoded"]))
+        for gi in range(len(d["guide_encoded"])):
+            sel = c["hit_guide"] == gi
+            assert res[gi] == list(zip(c["hit_pos"][sel].tolist(), c["hit_mm"][sel].tolist()))
+            assert cnt[gi] == int(c["counts"][gi])
+            assert ovf[gi] == bool(c["overflow"][gi])
+
+
+def _random_genome(seed, lens, n_frac=0.02):
+    rng = np.random.default_rng(seed)
+    total = int(sum(lens))
+    blocks, pos = [], 0
+    while pos < total:
+        pos += int(rng.integers(2_000, 60_000))
+        ln = int(rng.integers(1, 3_000))
+        if pos + ln >= total:
+            break
+        blocks.append((pos, pos + ln))
+        pos += ln
+    g = _native.synth_genome(seed, lens, blocks, thresholds=(76, 128, 180))
+    return g, rng
+
+
+def _plant(genome, rng, guide, pam, n_sites, max_sub):
+    """Plant sites of `guide` + a concrete PAM on both strands in place."""
+    comp = {"A": "T", "C": "G", "G": "C", "T": "A"}
+    expand = {"A": "A", "C": "C", "G": "G", "T": "T", "R": "AG", "Y": "CT", "M": "AC",
+              "K": "GT", "S": "CG", "W": "AT", "H": "ACT", "B": "CGT", "V": "ACG", "D": "AGT",
+              "N": "ACGT"}
+    fwd, rc = genome["genome_forward"], genome["genome_rc"]
+    offs, lens = genome["chrom_offsets"], genome["chrom_lengths"]
+    code = {"A": 0, "C": 1, "G": 2, "T": 3}
+    for _ in range(n_sites):
+        s = list(guide)
+        for p in rng.choice(20, size=int(rng.integers(0, max_sub + 1)), replace=False):
+            s[p] = rng.choice([b for b in "ACGT" if b != s[p]])
+        site = "".join(s) + "".join(rng.choice(list(expand[c])) for c in pam)
+        if rng.random() < 0.5:
+            site = "".join(comp[b] for b in reversed(site))
+        ci = int(rng.integers(0, len(lens)))
+        at = int(offs[ci] + rng.integers(0, lens[ci] - len(site)))
+        for k, b in enumerate(site):
+            p = at + k
+            v = code[b]
+            fwd[p >> 4] = (fwd[p >> 4] & ~np.uint32(3 << ((p & 15) * 2))) | np.uint32(v << ((p & 15) * 2))
+            q = int(offs[ci] + lens[ci] - 1 - (p - offs[ci]))
+            rc[q >> 4] = (rc[q >> 4] & ~np.uint32(3 << ((q & 15) * 2))) | np.uint32((3 - v) << ((q & 15) * 2))
+            nm = genome["n_mask"]
+            nm[p >> 3] &= np.uint8(~(1 << (7 - (p & 7))) & 0xFF)
+
+
+MIXED_PAMS = ["NGG", "NG", "NNGRRT", "NNNRRT", "NRN", "TTTV", "SGG", "NAG", "G", "NNNNNN"]
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_random_mixed_pam_keys_equal_oracle(seed):
+    genome, rng = _random_genome(seed, [700_000, 33, 410_000, 1_234_567])
+    seqs, pams = [], []
+    for i in range(48):
+        s = "".join(rng.choice(list("ACGT"), 20))
+        pam = MIXED_PAMS[i % len(MIXED_PAMS)]
+        _plant(genome, rng, s, pam, 6, 5)
+        seqs.append(s)
+        pams.append(pam)
+    exp = oracle_keys(genome, seqs, pams, 5)
+    assert exp.size > 100
+    f = beguidedoff(None, max_mismatches=5, genome_data=genome)
+    try:
+        for mode in (0, 1):
+            f.scan_mode = mode
+            got = f._scan(seqs, pams)
+            assert got.size == exp.size and np.array_equal(got, exp), mode
+    finally:
+        f.close()
+
+
+def test_large_genome_sampled_ranges_equal_oracle():
+    """96 Mbp, 64 NGG guides: full GPU key set; the oracle re-scans four
+    sampled 300 kbp ranges per strand and every planted site is found."""
+    genome, rng = _random_genome(5, [40_000_000, 56_000_000], n_frac=0.05)
+    seqs = ["".join(rng.choice(list("ACGT"), 20)) for _ in range(64)]
+    for s in seqs[:16]:
+        _plant(genome, rng, s, "NGG", 25, 3)
+    f = beguidedoff(None, max_mismatches=4, genome_data=genome)
+    try:
+        got = f._scan(seqs, ["NGG"] * len(seqs))
+    finally:
+        f.close()
+    row, slot, pos, mm = _native.split_keys(got)
+    gv = np.array([O.encode_guide(s) for s in seqs], dtype=np.uint64)
+    pm = np.tile(np.array([15, 4, 4, 0, 0, 0], dtype=np.uint8), (len(seqs), 1))
+    pl = np.full(len(seqs), 3, dtype=np.uint8)
+    p3 = np.ones(len(seqs), dtype=np.uint8)
+    fwd, rc = O.prepare_n_masks(genome)
+    tb = genome["total_bp"]
+    for s_i, (arr, nm, ne) in enumerate(((genome["genome_forward"], fwd, 0),
+                                         (genome["genome_rc"], rc, 3))):
+        for a in rng.integers(0, tb - 400_000, 4).tolist():
+            b = a + 300_000
+            _, keys = O.scan_strand(arr, tb, nm, gv, pm, pl, p3, 4, ne, a, b)
+            eg, ep, em = O.split_keys(keys)
+            sel = (slot == s_i) & (pos >= a) & (pos < b)
+            assert np.array_equal(row[sel], eg) and np.array_equal(pos[sel], ep)
+            assert np.array_equal(mm[sel], em)
+    assert int(((row < 16) & (mm <= 3)).sum()) >= 16 * 25
+
+
+def test_capi_error_paths():
+    L = _native.lib()
+    h = ctypes.c_void_p()
+    assert L.bgo_genome_create(None, 0, 0, None, 0, 0, None, ctypes.byref(h)) == _native.BGO_ERR_ARG
+    arr = np.zeros(4, dtype=np.uint32)
+    assert L.bgo_genome_create(arr.ctypes.data, 4, 1 << 33, None, 0, 0, None,
+                               ctypes.byref(h)) == _native.BGO_ERR_ARG
+    assert "total_bp" in _native.last_error()
+    eng = _native.Engine(0)
+    n = ctypes.c_int64()
+    assert L.bgo_scan_collect(eng.handle, None, 0, ctypes.byref(n), None) == _native.BGO_ERR_STATE
+    s = _native.Strand(np.arange(100, dtype=np.uint32), 1600)
+    assert s.info()["total_bp"] == 1600 and not s.info()["has_n_mask"]
+    plan = _native.Plan(eng, np.array([1, 2, 3], dtype=np.uint64),
+                        np.array([[15, 4, 4, 0, 0, 0], [15, 4, 4, 0, 0, 0], [4, 0, 0, 0, 0, 0]],
+                                 dtype=np.uint8), np.array([3, 3, 0], dtype=np.uint8),
+                        np.ones(3, dtype=np.uint8))
+    assert plan.info() == {"n_families": 1, "n_guides": 3}
+    ne = np.array([5], dtype=np.int32)
+    arrp = (ctypes.c_void_p * 1)(s.handle.value)
+    assert L.bgo_scan_launch(eng.handle, plan.handle, arrp, ne.ctypes.data, 1, 4, 0,
+                             None) == _native.BGO_ERR_ARG
+    keys = eng.scan(plan, [s], [0], 20)   # max_mm 20: every NGG site, rows 0 and 1
+    counts, exp = O.scan_strand(arr_words := np.arange(100, dtype=np.uint32), 1600, None,
+                                plan.guides, plan.pam_masks, plan.pam_lens, plan.pam_3prime,
+                                20, 0)
+    assert keys.size == exp.size > 0 and counts[2] == 0
+    assert np.array_equal(_native.split_keys(keys)[2], O.split_keys(exp)[1])
+    plan.close()
+    s.close()
+    eng.close()
+
+
+def test_hit_buffer_growth_keeps_exact_output():
+    """More hits than the initial device buffer: the engine grows and re-runs."""
+    unit = "T" + "ACGTACGTACGTACGTACGT"[1:] + "AGG"
+    case_seq = unit * 1_100_000 + "A" * 30
+    from beguidedoff_gb300.genome_converter import encode_chromosomes
+
+    g = encode_chromosomes([("chr1", case_seq.encode())])
+    f = beguidedoff(None, max_mismatches=4, genome_data=g)
+    try:
+        cap0 = f._engine.info()["hit_capacity"]
+        got = f._scan(["ACGTACGTACGTACGTACGT"], ["NGG"])
+        assert f._engine.info()["hit_capacity"] > cap0
+    finally:
+        f.close()
+    exp = oracle_keys(g, ["ACGTACGTACGTACGTACGT"], ["NGG"], 4)
+    assert exp.size > cap0 and np.array_equal(got, exp)

@@ -1,0 +1,90 @@
+"""Shared utilities against the reference's unit-test answers
+(tests/test_encoding.py, test_pam.py, test_scoring.py, test_base_editing.py)."""
+import numpy as np
+import pytest
+
+from beguidedoff_gb300 import encoding as E
+from beguidedoff_gb300 import pam as P
+from beguidedoff_gb300 import scoring as S
+from beguidedoff_gb300 import base_editing as B
+from beguidedoff_gb300.types import GuideInput
+
+
+def test_encoding_known_answers():
+    assert E.decode_dna(E.encode_dna("ACGTACGTNNACGT")) == "ACGTACGTAAACGT"
+    assert E.reverse_complement_seq("ATCG") == "CGAT"
+    enc = E.encode_dna("ACGT" * 10)
+    assert np.array_equal(E.unpack_uint32_to_2bit(E.pack_2bit_to_uint32(enc), 40), enc)
+    g = E.encode_dna("ACGTACGTACGTACGTACGT")
+    assert np.array_equal(E.decode_guide_64bit(E.encode_guide_64bit(g)), g)
+    va = E.encode_guide_64bit(g)
+    vb = E.encode_guide_64bit(E.encode_dna("ACGTACGTACGTACGTACGA"))
+    vc = E.encode_guide_64bit(E.encode_dna("TCGTACGTACGTACGTACGT"))
+    assert E.hamming_distance_2bit(va, vb) == 1
+    assert E.mismatch_positions_2bit(va, vb) == [20]
+    assert E.mismatch_positions_2bit(va, vc) == [1]
+    assert E.encode_dna("acgtRYn").tolist() == [0, 1, 2, 3, 0, 0, 0]
+
+
+def test_extract_windows_matches_scalar():
+    rng = np.random.default_rng(3)
+    bases = rng.integers(0, 4, 1000).astype(np.uint8)
+    packed = E.pack_2bit_to_uint32(bases)
+    starts = rng.integers(0, 970, 50)
+    w = E.extract_windows(packed, starts, 20)
+    for i, s in enumerate(starts):
+        assert np.array_equal(w[i], bases[s:s + 20])
+        assert np.array_equal(E.extract_window(packed, int(s), 20), bases[s:s + 20])
+
+
+def test_pam_known_answers():
+    P.validate_pam("NGG")
+    P.validate_pam("NNGRRT")
+    with pytest.raises(ValueError):
+        P.validate_pam("NNNNNNN")
+    with pytest.raises(ValueError):
+        P.validate_pam("NGX")
+    m = P.encode_pam_mask("NGG")
+    assert m.tolist() == [15, 4, 4, 0, 0, 0]
+    pams = P.all_possible_pams("NGG")
+    assert len(pams) == 4 and "AGG" in pams and "GGG" in pams
+    gs = [GuideInput("g1", "A" * 20, "NGG", "3prime", 4, 8, "CBE"),
+          GuideInput("g2", "A" * 20, "NNGRRT", "3prime", 4, 8, "CBE"),
+          GuideInput("g3", "A" * 20, "NGG", "3prime", 4, 8, "ABE")]
+    groups = P.group_guides_by_pam(gs)
+    assert len(groups[("NGG", "3prime")]) == 2 and len(groups[("NNGRRT", "3prime")]) == 1
+
+
+def test_cctop_known_answers():
+    assert S.calculate_cctop_score([]) == 0.0
+    assert abs(S.calculate_cctop_score([20]) - 1.2 ** 20) < 1e-9
+    assert abs(S.calculate_cctop_score([1, 5, 10]) - (1.2 + 1.2 ** 5 + 1.2 ** 10)) < 1e-9
+
+
+def test_vectorised_cctop_is_bit_exact():
+    """cctop_from_masks equals Python's sum over ascending positions for
+    every mask with up to 6 mismatches and a random sample of the rest."""
+    from itertools import combinations
+
+    masks = [0]
+    for k in range(1, 7):
+        masks += [sum(1 << (p - 1) for p in c) for c in combinations(range(1, 21), k)]
+    rng = np.random.default_rng(0)
+    masks += rng.integers(0, 1 << 20, 20000).tolist()
+    masks = np.array(masks, dtype=np.int64)
+    got = S.cctop_from_masks(masks)
+    for m, v in zip(masks.tolist(), got.tolist()):
+        exp = S.calculate_cctop_score([p for p in range(1, 21) if (m >> (p - 1)) & 1])
+        assert v == exp
+
+
+def test_base_editing_known_answers():
+    seq = "ACGTACGTACGTACGTACGT"
+    assert 6 in B.editable_base_in_window(seq, "CBE", 4, 8)
+    pos = B.editable_base_in_window(seq, "ABE", 1, 5)
+    assert 1 in pos and 5 in pos
+    assert B.editable_base_in_window("G" * 20, "CBE", 1, 10) == []
+    assert B.get_trinucleotide_contexts("ACGTACGT", [3]) == ["CGT"]
+    assert B.has_editable_base(seq, "CBE", 4, 8)
+    with pytest.raises(ValueError):
+        B.editable_base_in_window(seq, "XBE", 4, 8)
