@@ -25,7 +25,11 @@ EXPORTED = [
     "bgo_engine_destroy", "bgo_plan_create", "bgo_plan_destroy", "bgo_plan_info",
     "bgo_scan_launch", "bgo_scan_collect", "bgo_engine_reserve", "bgo_search_genome",
     "bgo_engine_info", "bgo_synth_genome", "bgo_probe_int_throughput", "bgo_scan_stats",
+    "bgo_scan_noalloc",
 ]
+
+NOALLOC_MAX_GUIDES = 2048
+NOALLOC_MAX_HITS = 1 << 20
 
 
 class NativeLibraryMissing(RuntimeError):
@@ -63,6 +67,8 @@ _SIGS = {
     "bgo_scan_launch": ([_P, _P, _P, _P, _I32, _I32, _I32, _P], ctypes.c_int),
     "bgo_scan_collect": ([_P, _P, _I64, ctypes.POINTER(_I64), _P], ctypes.c_int),
     "bgo_scan_stats": ([_P, ctypes.POINTER(_I64), _P], ctypes.c_int),
+    "bgo_scan_noalloc": ([_P, _P, _I32, _P, _P, _P, _P, _I32, _I32, _P, _I64,
+                          ctypes.POINTER(_I64), _P], ctypes.c_int),
     "bgo_engine_reserve": ([_P, _I64], ctypes.c_int),
     "bgo_search_genome": ([_P, _P, _P, _P, _P, _P, _I32, _I32, _I32, _I64, _P, _P, _P, _P],
                           ctypes.c_int),

@@ -147,6 +147,31 @@ int bgo_search_genome(bgo_engine *engine, const bgo_genome *strand, const uint64
 int bgo_engine_info(const bgo_engine *engine, int64_t *hit_capacity, int64_t *n_launches);
 
 /*
+ * The scan for callers that cannot allocate device memory: programs whose own
+ * allocator already owns the GPU's memory, and latency-critical loops where a
+ * cudaMalloc/cudaFree would synchronise the device.  No counterpart in the
+ * reference.  It allocates nothing (device or host): its guide tables,
+ * counters and a key buffer live in one static device array of about 8.1 MB
+ * that every GPU loading this library reserves until the process exits.  The
+ * first call on a device looks that array's address up (make it before any
+ * stream capture); calls whose work overlaps on the GPU share the array and
+ * race, so serialise them.  Limits: n_guides <= BGO_NOALLOC_MAX_GUIDES
+ * (larger values return BGO_ERR_ARG), at most BGO_NOALLOC_MAX_HITS hits per
+ * call (more return BGO_ERR_OOM with the exact count in *n_hits).
+ * Inputs and outputs are the caller's: strands as for bgo_scan_launch, guide
+ * rows as for bgo_plan_create (host arrays); on success *n_hits is the exact
+ * hit count and, when it is <= capacity, `keys` (host) receives all hit keys in
+ * ascending order, the same keys bgo_scan_collect returns.
+ */
+#define BGO_NOALLOC_MAX_GUIDES 2048
+#define BGO_NOALLOC_MAX_HITS (1 << 20)
+int bgo_scan_noalloc(const bgo_genome *const *strands, const int32_t *n_encoded,
+                     int32_t n_strands, const uint64_t *guide_encoded, const uint8_t *pam_masks,
+                     const uint8_t *pam_lens, const uint8_t *pam_3prime, int32_t n_guides,
+                     int32_t max_mismatches, uint64_t *keys, int64_t capacity, int64_t *n_hits,
+                     void *stream);
+
+/*
  * Seeded synthetic genome in the reference .npz layout (what
  * beguidedoff/genome_converter.py:15-108 writes for the equivalent FASTA):
  * chromosomes of the given lengths concatenated, bases drawn per position from
