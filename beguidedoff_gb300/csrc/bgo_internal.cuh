@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/bgo.h"
 
@@ -66,6 +67,39 @@ struct ScanParams {
     int64_t tiles_total;
 };
 
+// Segment-indexed scan (scan mode 2): 512 threads, two plane words (64
+// positions) per thread per tile.
+constexpr int kSeedThreads = 512;
+constexpr int kSeedWpt = 2;
+constexpr int kSeedTileSites = kSeedThreads * kSeedWpt * 32;  // 32768 positions
+constexpr int kSeedTileWords = kSeedTileSites / 32 + 4;
+constexpr int kMaxSeg = 20;
+constexpr int kMaxKeyLen = 6;
+
+struct SeedSeg {
+    uint8_t start, len, klen, pad;
+    uint32_t off;  // first bucket offset of this segment in the offsets table
+};
+
+struct SeedFam {
+    int32_t nseg;
+    uint32_t list_off;  // this family's lists: segment j at list_off + j * family size
+    uint32_t pad[2];
+    SeedSeg seg[kMaxSeg];
+};
+
+struct SeedArgs {
+    const SeedFam *fams;
+    const uint32_t *offsets;
+    const uint16_t *lists;
+    int32_t n_fams, n_guides, n_offsets, n_lists;
+};
+
+inline int64_t seed_tiles_for(int64_t total_bp) {
+    int64_t valid = total_bp - kSiteSpan;
+    return valid > 0 ? (valid + kSeedTileSites - 1) / kSeedTileSites : 0;
+}
+
 void set_error(const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
 
@@ -111,7 +145,20 @@ struct bgo_plan {
     bgo::FamilyDesc *d_fams;
     bgo::GuideRec *d_guides;
     bgo::FamilyDesc *h_fams;  // host copy (n_families)
+    bgo::GuideRec *h_guides;  // host copy (n_active)
+    // segment index for one max_mismatches value, built on first use
+    int seed_k;               // -1000 = not built
+    int seed_ok;              // 0: the filter does not apply to this K
+    unsigned char *d_seed;    // device block: families | offsets | lists
+    bgo::SeedArgs seed;
 };
+
+namespace bgo {
+bool build_seed_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
+                      std::vector<SeedFam> &out_fams, std::vector<uint32_t> &offsets,
+                      std::vector<uint16_t> &lists);
+int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, cudaStream_t s);
+}  // namespace bgo
 
 struct bgo_engine {
     int device;

@@ -337,10 +337,13 @@ extern "C" int bgo_plan_create(bgo_engine *engine, const uint64_t *guide_encoded
     pl->n_active = (int32_t)recs.size();
     pl->n_families = (int32_t)fams.size();
     pl->h_fams = new (std::nothrow) FamilyDesc[fams.size() + 1];
+    pl->h_guides = new (std::nothrow) GuideRec[recs.size() + 1];
+    pl->seed_k = -1000;
     cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = pl->h_fams ? cudaSuccess : cudaErrorMemoryAllocation;
+    cudaError_t e = (pl->h_fams && pl->h_guides) ? cudaSuccess : cudaErrorMemoryAllocation;
     if (e == cudaSuccess) {
         std::copy(fams.begin(), fams.end(), pl->h_fams);
+        std::copy(recs.begin(), recs.end(), pl->h_guides);
         e = cudaMalloc(&pl->d_fams, sizeof(FamilyDesc) * (fams.size() + 1));
     }
     if (e == cudaSuccess) e = cudaMalloc(&pl->d_guides, sizeof(GuideRec) * (recs.size() + 1));
@@ -365,6 +368,8 @@ extern "C" int bgo_plan_destroy(bgo_plan *pl) {
     if (pl->d_fams) cudaFree(pl->d_fams);
     if (pl->d_guides) cudaFree(pl->d_guides);
     delete[] pl->h_fams;
+    delete[] pl->h_guides;
+    if (pl->d_seed) cudaFree(pl->d_seed);
     delete pl;
     return BGO_OK;
 }
@@ -391,12 +396,55 @@ static void fill_strand(StrandDesc &d, const bgo_genome *g, int32_t n_encoded, i
     d.pad = 0;
 }
 
+// Builds (once per max_mismatches value) and uploads the plan's segment
+// index.  Returns 1 when the index applies, 0 when the scan must compare every
+// guide (mode 1), or a negative BGO_ERR_*.
+static int seed_prepare(bgo_plan *pl, int K, cudaStream_t s) {
+    if (pl->seed_k == K) return pl->seed_ok;
+    if (pl->d_seed) {
+        BGO_CUDA(cudaStreamSynchronize(s));
+        cudaFree(pl->d_seed);
+        pl->d_seed = nullptr;
+    }
+    pl->seed_k = K;
+    pl->seed_ok = 0;
+    std::vector<SeedFam> sf;
+    std::vector<uint32_t> offs;
+    std::vector<uint16_t> lists;
+    if (!build_seed_index(pl->h_fams, pl->n_families, pl->h_guides, K, sf, offs, lists)) return 0;
+    const size_t b_f = sizeof(SeedFam) * sf.size();
+    const size_t b_o = sizeof(uint32_t) * offs.size();
+    const size_t b_l = sizeof(uint16_t) * lists.size();
+    const size_t o_o = (b_f + 255) / 256 * 256, o_l = o_o + (b_o + 255) / 256 * 256;
+    SeedArgs sa{};
+    sa.n_fams = (int32_t)sf.size();
+    sa.n_guides = pl->n_active;
+    sa.n_offsets = (int32_t)offs.size();
+    sa.n_lists = (int32_t)lists.size();
+    // the whole index and guide table must fit next to the tile in shared memory
+    const size_t smem = sizeof(uint32_t) * 3 * kSeedTileWords + sizeof(uint16_t) * kSeedTileSites +
+                        b_f + 16 + sizeof(uint4) * sa.n_guides + b_o + b_l + 16;
+    if (smem > 200 * 1024) return 0;
+    BGO_CUDA(cudaMalloc(&pl->d_seed, o_l + b_l + 16));
+    BGO_CUDA(cudaMemcpyAsync(pl->d_seed, sf.data(), b_f, cudaMemcpyHostToDevice, s));
+    BGO_CUDA(cudaMemcpyAsync(pl->d_seed + o_o, offs.data(), b_o, cudaMemcpyHostToDevice, s));
+    if (b_l)
+        BGO_CUDA(cudaMemcpyAsync(pl->d_seed + o_l, lists.data(), b_l, cudaMemcpyHostToDevice, s));
+    BGO_CUDA(cudaStreamSynchronize(s));
+    sa.fams = reinterpret_cast<const SeedFam *>(pl->d_seed);
+    sa.offsets = reinterpret_cast<const uint32_t *>(pl->d_seed + o_o);
+    sa.lists = reinterpret_cast<const uint16_t *>(pl->d_seed + o_l);
+    pl->seed = sa;
+    pl->seed_ok = 1;
+    return 1;
+}
+
 extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
                                const bgo_genome *const *strands, const int32_t *n_encoded,
                                int32_t n_strands, int32_t max_mismatches, int32_t mode,
                                void *stream) {
     if (!engine || !plan || !strands || !n_encoded || n_strands < 1 || n_strands > 2 ||
-        (mode != 0 && mode != 1)) {
+        mode < 0 || mode > 2) {
         set_error("bgo_scan_launch: invalid argument");
         return BGO_ERR_ARG;
     }
@@ -439,6 +487,19 @@ extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
                 engine->launches++;
             }
         }
+    } else if (mode == 2 && seed_prepare(const_cast<bgo_plan *>(plan), max_mismatches, s) == 1) {
+        for (int i = 0; i < n_strands; ++i) {
+            fill_strand(p.strand[i], strands[i], n_encoded[i], i);
+            p.strand[i].n_tiles = seed_tiles_for(strands[i]->total_bp);
+        }
+        p.n_strands = n_strands;
+        p.tiles_total = p.strand[0].n_tiles + (n_strands > 1 ? p.strand[1].n_tiles : 0);
+        if (p.tiles_total == 0) return BGO_OK;
+        p.fam_begin = 0;
+        p.fam_end = plan->n_families;
+        const int rc = launch_seed_kernel(p, plan->seed, engine->sm_count, s);
+        if (rc != BGO_OK) return rc;
+        engine->launches++;
     } else {
         for (int i = 0; i < n_strands; ++i) fill_strand(p.strand[i], strands[i], n_encoded[i], i);
         p.n_strands = n_strands;

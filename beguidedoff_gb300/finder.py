@@ -91,7 +91,7 @@ class beguidedoff:
     def __init__(self, genome_path: str, max_mismatches: int = 4, scoring_method: str = "CCTOP",
                  device: Optional[str] = None, n_top_offtargets: int = 3,
                  results_per_guide: int = 10240, max_results_per_guide: Optional[int] = None,
-                 genome_data: Optional[dict] = None, scan_mode: int = 1):
+                 genome_data: Optional[dict] = None, scan_mode: int = 2):
         self.genome_path = genome_path
         self.max_mismatches = max_mismatches
         if scoring_method.upper() != "CCTOP":

@@ -24,7 +24,7 @@ def _lib():
     assert _native.device_count() >= 1
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 @pytest.mark.parametrize("name", FINDER_CASES)
 def test_finder_tables_match_reference(name, mode):
     case = Case(name)
@@ -145,7 +145,7 @@ def test_random_mixed_pam_keys_equal_oracle(seed):
     assert exp.size > 100
     f = beguidedoff(None, max_mismatches=5, genome_data=genome)
     try:
-        for mode in (0, 1):
+        for mode in (0, 1, 2):
             f.scan_mode = mode
             got = f._scan(seqs, pams)
             assert got.size == exp.size and np.array_equal(got, exp), mode
