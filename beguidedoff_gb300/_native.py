@@ -25,7 +25,7 @@ EXPORTED = [
     "bgo_engine_destroy", "bgo_plan_create", "bgo_plan_destroy", "bgo_plan_info",
     "bgo_scan_launch", "bgo_scan_collect", "bgo_engine_reserve", "bgo_search_genome",
     "bgo_engine_info", "bgo_synth_genome", "bgo_probe_int_throughput", "bgo_scan_stats",
-    "bgo_scan_noalloc",
+    "bgo_scan_noalloc", "bgo_graph_create", "bgo_graph_launch", "bgo_graph_destroy",
 ]
 
 NOALLOC_MAX_GUIDES = 2048
@@ -67,6 +67,9 @@ _SIGS = {
     "bgo_scan_launch": ([_P, _P, _P, _P, _I32, _I32, _I32, _P], ctypes.c_int),
     "bgo_scan_collect": ([_P, _P, _I64, ctypes.POINTER(_I64), _P], ctypes.c_int),
     "bgo_scan_stats": ([_P, ctypes.POINTER(_I64), _P], ctypes.c_int),
+    "bgo_graph_create": ([_P, _P, _P, _P, _I32, _I32, _I32, _PP], ctypes.c_int),
+    "bgo_graph_launch": ([_P, _P], ctypes.c_int),
+    "bgo_graph_destroy": ([_P], ctypes.c_int),
     "bgo_scan_noalloc": ([_P, _P, _I32, _P, _P, _P, _P, _I32, _I32, _P, _I64,
                           ctypes.POINTER(_I64), _P], ctypes.c_int),
     "bgo_engine_reserve": ([_P, _I64], ctypes.c_int),
@@ -331,6 +334,35 @@ class Engine:
     def close(self):
         if self.handle is not None and self.handle.value:
             lib().bgo_engine_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Graph:
+    """A scan captured once into a CUDA graph; replay() rescans (keep the
+    engine, plan and strands alive and do not reserve the engine meanwhile)."""
+
+    def __init__(self, engine, plan, strands, n_encoded, max_mismatches, mode=2):
+        arr = (ctypes.c_void_p * len(strands))(*[s.handle.value for s in strands])
+        ne = np.ascontiguousarray(n_encoded, dtype=np.int32)
+        h = ctypes.c_void_p()
+        check(lib().bgo_graph_create(engine.handle, plan.handle, arr, ptr(ne), len(strands),
+                                     int(max_mismatches), int(mode), ctypes.byref(h)),
+              "bgo_graph_create")
+        self.handle = h
+        self._keep = (engine, plan, strands)
+
+    def replay(self, stream=None):
+        check(lib().bgo_graph_launch(self.handle, stream), "bgo_graph_launch")
+
+    def close(self):
+        if self.handle is not None and self.handle.value:
+            lib().bgo_graph_destroy(self.handle)
         self.handle = None
 
     def __del__(self):

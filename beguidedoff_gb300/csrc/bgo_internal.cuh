@@ -67,12 +67,11 @@ struct ScanParams {
     int64_t tiles_total;
 };
 
-// Segment-indexed scan (scan mode 2): 512 threads, two plane words (64
-// positions) per thread per tile.
-constexpr int kSeedThreads = 512;
-constexpr int kSeedWpt = 2;
-constexpr int kSeedTileSites = kSeedThreads * kSeedWpt * 32;  // 32768 positions
-constexpr int kSeedTileWords = kSeedTileSites / 32 + 4;
+// Segment-indexed scan (scan mode 2): independent warps, each streaming chunks
+// of kSeedChunkSites positions; max_mismatches up to kSeedMaxK.
+constexpr int kSeedThreads = 256;
+constexpr int kSeedChunkSites = 2048;
+constexpr int kSeedMaxK = 7;
 constexpr int kMaxSeg = 20;
 constexpr int kMaxKeyLen = 6;
 
@@ -88,16 +87,18 @@ struct SeedFam {
     SeedSeg seg[kMaxSeg];
 };
 
+// Bucket entry: guide planes h, l (20 bits each) with the family-local guide
+// index split over the top 12 bits of both words.
 struct SeedArgs {
     const SeedFam *fams;
-    const uint32_t *offsets;
-    const uint16_t *lists;
+    const uint32_t *offsets;  // per bucket: entry start | count << 16
+    const uint2 *entries;
     int32_t n_fams, n_guides, n_offsets, n_lists;
 };
 
 inline int64_t seed_tiles_for(int64_t total_bp) {
     int64_t valid = total_bp - kSiteSpan;
-    return valid > 0 ? (valid + kSeedTileSites - 1) / kSeedTileSites : 0;
+    return valid > 0 ? (valid + kSeedChunkSites - 1) / kSeedChunkSites : 0;
 }
 
 void set_error(const std::string &msg);
@@ -117,12 +118,18 @@ inline int64_t tiles_for(int64_t total_bp) {
     return valid > 0 ? ceil_div(valid, kTileSites) : 0;
 }
 
-// Plane words needed so every tile load [t*256, t*256 + kTileWords) is inside.
+// Plane words needed so every tile load [t*256, t*256 + kTileWords) of the
+// plain kernel and every 16-byte-aligned chunk copy of the segment-indexed
+// kernel ([c*64, c*64 + 68) words, see bgo_seed.cu) is inside the buffer.
 inline int64_t plane_words_for(int64_t total_bp) {
     int64_t t = tiles_for(total_bp);
     int64_t need = t * (kTileSites / 32) + kTileWords;
+    int64_t valid = total_bp - kSiteSpan;
+    int64_t chunks = valid > 0 ? ceil_div(valid, 2048) : 0;
+    int64_t need2 = chunks * 64 + 68;
     int64_t cover = ceil_div(total_bp > 0 ? total_bp : 1, 32) + 4;
     int64_t w = need > cover ? need : cover;
+    w = w > need2 ? w : need2;
     return (w + 63) / 64 * 64;
 }
 
@@ -156,7 +163,8 @@ struct bgo_plan {
 namespace bgo {
 bool build_seed_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
                       std::vector<SeedFam> &out_fams, std::vector<uint32_t> &offsets,
-                      std::vector<uint16_t> &lists);
+                      std::vector<uint2> &entries);
+size_t seed_smem_bytes(const SeedArgs &sa);
 int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, cudaStream_t s);
 }  // namespace bgo
 

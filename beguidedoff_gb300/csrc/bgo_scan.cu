@@ -410,30 +410,28 @@ static int seed_prepare(bgo_plan *pl, int K, cudaStream_t s) {
     pl->seed_ok = 0;
     std::vector<SeedFam> sf;
     std::vector<uint32_t> offs;
-    std::vector<uint16_t> lists;
-    if (!build_seed_index(pl->h_fams, pl->n_families, pl->h_guides, K, sf, offs, lists)) return 0;
+    std::vector<uint2> ents;
+    if (!build_seed_index(pl->h_fams, pl->n_families, pl->h_guides, K, sf, offs, ents)) return 0;
     const size_t b_f = sizeof(SeedFam) * sf.size();
+    const size_t b_e = sizeof(uint2) * ents.size();
     const size_t b_o = sizeof(uint32_t) * offs.size();
-    const size_t b_l = sizeof(uint16_t) * lists.size();
-    const size_t o_o = (b_f + 255) / 256 * 256, o_l = o_o + (b_o + 255) / 256 * 256;
+    const size_t o_e = (b_f + 255) / 256 * 256, o_o = o_e + (b_e + 255) / 256 * 256;
     SeedArgs sa{};
     sa.n_fams = (int32_t)sf.size();
     sa.n_guides = pl->n_active;
     sa.n_offsets = (int32_t)offs.size();
-    sa.n_lists = (int32_t)lists.size();
-    // the whole index and guide table must fit next to the tile in shared memory
-    const size_t smem = sizeof(uint32_t) * 3 * kSeedTileWords + sizeof(uint16_t) * kSeedTileSites +
-                        b_f + 16 + sizeof(uint4) * sa.n_guides + b_o + b_l + 16;
-    if (smem > 200 * 1024) return 0;
-    BGO_CUDA(cudaMalloc(&pl->d_seed, o_l + b_l + 16));
+    sa.n_lists = (int32_t)ents.size();
+    // the whole index must fit in shared memory beside the warps' chunk slices
+    if (seed_smem_bytes(sa) > 200 * 1024) return 0;
+    BGO_CUDA(cudaMalloc(&pl->d_seed, o_o + b_o + 16));
     BGO_CUDA(cudaMemcpyAsync(pl->d_seed, sf.data(), b_f, cudaMemcpyHostToDevice, s));
+    if (b_e)
+        BGO_CUDA(cudaMemcpyAsync(pl->d_seed + o_e, ents.data(), b_e, cudaMemcpyHostToDevice, s));
     BGO_CUDA(cudaMemcpyAsync(pl->d_seed + o_o, offs.data(), b_o, cudaMemcpyHostToDevice, s));
-    if (b_l)
-        BGO_CUDA(cudaMemcpyAsync(pl->d_seed + o_l, lists.data(), b_l, cudaMemcpyHostToDevice, s));
     BGO_CUDA(cudaStreamSynchronize(s));
     sa.fams = reinterpret_cast<const SeedFam *>(pl->d_seed);
+    sa.entries = reinterpret_cast<const uint2 *>(pl->d_seed + o_e);
     sa.offsets = reinterpret_cast<const uint32_t *>(pl->d_seed + o_o);
-    sa.lists = reinterpret_cast<const uint16_t *>(pl->d_seed + o_l);
     pl->seed = sa;
     pl->seed_ok = 1;
     return 1;
@@ -487,7 +485,12 @@ extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
                 engine->launches++;
             }
         }
-    } else if (mode == 2 && seed_prepare(const_cast<bgo_plan *>(plan), max_mismatches, s) == 1) {
+    }
+    const int seeded = mode == 2 ? seed_prepare(const_cast<bgo_plan *>(plan), max_mismatches, s) : 0;
+    if (seeded < 0) return seeded;
+    if (mode == 0) {
+        // launched above
+    } else if (seeded == 1) {
         for (int i = 0; i < n_strands; ++i) {
             fill_strand(p.strand[i], strands[i], n_encoded[i], i);
             p.strand[i].n_tiles = seed_tiles_for(strands[i]->total_bp);
@@ -512,6 +515,73 @@ extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
         BGO_CUDA(cudaGetLastError());
         engine->launches++;
     }
+    return BGO_OK;
+}
+
+struct bgo_graph {
+    int device;
+    bgo_engine *engine;
+    cudaGraphExec_t exec;
+    int64_t launches_per_replay;
+};
+
+extern "C" int bgo_graph_create(bgo_engine *engine, const bgo_plan *plan,
+                                const bgo_genome *const *strands, const int32_t *n_encoded,
+                                int32_t n_strands, int32_t max_mismatches, int32_t mode,
+                                bgo_graph **out) {
+    if (!out) return BGO_ERR_ARG;
+    *out = nullptr;
+    if (!engine) return BGO_ERR_ARG;
+    BGO_CUDA(cudaSetDevice(engine->device));
+    cudaStream_t cs = nullptr;
+    BGO_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    // one ordinary launch first: builds the segment index, sets kernel
+    // attributes and validates the arguments outside the capture
+    int rc = bgo_scan_launch(engine, plan, strands, n_encoded, n_strands, max_mismatches, mode, cs);
+    cudaError_t e = rc == BGO_OK ? cudaStreamSynchronize(cs) : cudaSuccess;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const int64_t before = engine->launches;
+    if (rc == BGO_OK && e == cudaSuccess)
+        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (rc == BGO_OK && e == cudaSuccess) {
+        rc = bgo_scan_launch(engine, plan, strands, n_encoded, n_strands, max_mismatches, mode, cs);
+        cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+        if (e2 != cudaSuccess && rc == BGO_OK) e = e2;
+    }
+    if (rc == BGO_OK && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    if (rc != BGO_OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "bgo_graph_create");
+    bgo_graph *g = new (std::nothrow) bgo_graph();
+    if (!g) {
+        cudaGraphExecDestroy(exec);
+        return BGO_ERR_OOM;
+    }
+    g->device = engine->device;
+    g->engine = engine;
+    g->exec = exec;
+    g->launches_per_replay = engine->launches - before;
+    engine->launches = before;  // the capture itself ran nothing
+    *out = g;
+    return BGO_OK;
+}
+
+extern "C" int bgo_graph_launch(bgo_graph *g, void *stream) {
+    if (!g) return BGO_ERR_ARG;
+    BGO_CUDA(cudaSetDevice(g->device));
+    BGO_CUDA(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+    g->engine->launched = 1;
+    g->engine->launches += g->launches_per_replay;
+    return BGO_OK;
+}
+
+extern "C" int bgo_graph_destroy(bgo_graph *g) {
+    if (!g) return BGO_OK;
+    cudaSetDevice(g->device);
+    cudaGraphExecDestroy(g->exec);
+    delete g;
     return BGO_OK;
 }
 

@@ -13,12 +13,20 @@
 // A candidate reached through segment j is reported only if no earlier segment
 // also matches exactly, so each (position, guide) hit is emitted once.
 //
-// Layout.  One persistent CTA of 512 threads per half SM; each tile is 32,768
-// positions of one strand (two plane words per thread).  The PAM families'
-// segment indexes and guide planes are copied to shared memory once per CTA.
-// Per tile and family: bit-parallel PAM test of 64 positions per thread, CTA
-// compaction of the passing positions, then one thread per compacted position
-// walks its K + 1 buckets.  Hits are appended with one atomicAdd per warp.
+// Layout.  Warps work independently (no CTA barrier after the start): each
+// warp takes chunks of kSeedChunkSites positions of one strand, copies the
+// chunk's H/L/N words (+2 halo words) to its own shared-memory slice, tests the
+// PAM of 32 positions per lane and word with funnel shifts and LOP3, and
+// compacts the passing positions into its own list with one warp scan.  Then,
+// 32 positions per round (one per lane), each lane looks up its K + 1 bucket
+// descriptors (one shared load each), the warp scans the candidate counts and
+// every lane writes its candidates (entry, segment, lane) into the warp's
+// queue; the whole warp then compares the queued candidates 32 at a time,
+// reading the owning position's window from the warp's record slots.  Rounds
+// whose candidates exceed the queue fall back to each lane walking its own
+// buckets.  The segment layout is a compile-time function of K, and every
+// bucket entry carries the guide's two 20-bit planes.  Hits are appended with
+// one atomicAdd per warp.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,17 +36,40 @@
 
 namespace bgo {
 
+constexpr int kSeedWarps = kSeedThreads / 32;
+constexpr int kChunkRows = kSeedChunkSites / 1024;     // 32-position words per lane
+constexpr int kChunkWords = kSeedChunkSites / 32 + 4;  // 64 + halo, a multiple of 4 words
+constexpr int kChunkVecs = kChunkWords / 4;            // 16-byte copies per plane
+constexpr int kQueueCap = 512;                          // queued candidates per round
+// per warp: two chunk buffers (H, L, N planes), the compacted list, the round's
+// position records and the candidate queue
+constexpr size_t kBufBytes = 3 * kChunkWords * sizeof(uint32_t);
+constexpr size_t kListOff = 2 * kBufBytes;
+constexpr size_t kRecOff = (kListOff + kSeedChunkSites * sizeof(uint16_t) + 15) / 16 * 16;
+constexpr size_t kQueueOff = kRecOff + 32 * sizeof(uint4);
+constexpr size_t kWarpSliceBytes = (kQueueOff + kQueueCap * sizeof(uint32_t) + 15) / 16 * 16;
+static_assert(kChunkWords % 4 == 0, "chunk copies are whole 16-byte vectors");
+static_assert(kBufBytes % 16 == 0, "chunk buffers stay 16-byte aligned");
+
+// Asynchronous 16-byte global -> shared copy (completes at cp.async.wait_group).
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
 __device__ __forceinline__ uint32_t sfshr(uint32_t lo, uint32_t hi, uint32_t s) {
     return __funnelshift_r(lo, hi, s);
 }
 
 __device__ __forceinline__ uint32_t sallowed(uint32_t h, uint32_t l, uint32_t a) {
-    uint32_t r = 0;
-    if (a & 1u) r |= ~h & ~l;
-    if (a & 2u) r |= ~h & l;
-    if (a & 4u) r |= h & ~l;
-    if (a & 8u) r |= h & l;
-    return r;
+    const uint32_t m0 = 0u - (a & 1u), m1 = 0u - ((a >> 1) & 1u);
+    const uint32_t m2 = 0u - ((a >> 2) & 1u), m3 = 0u - ((a >> 3) & 1u);
+    return (~h & ~l & m0) | (~h & l & m1) | (h & ~l & m2) | (h & l & m3);
 }
 
 __device__ __forceinline__ void semit(uint64_t key, uint64_t *keys, int64_t cap,
@@ -53,89 +84,137 @@ __device__ __forceinline__ void semit(uint64_t key, uint64_t *keys, int64_t cap,
     if (slot < (unsigned long long)cap) keys[slot] = key;
 }
 
-// 20-bit H, L and gated N windows of compacted position s (tile-relative).
-struct SiteWin {
-    uint32_t h, l, n;
+// The K + 1 segments: start and key length (the segment's first <= 6 bases).
+template <int K>
+struct Seg {
+    static constexpr int S = K + 1;
+    static constexpr int q = kGuideLen / S, r = kGuideLen % S;
+    __host__ __device__ static constexpr int start(int j) { return j * q + (j < r ? j : r); }
+    __host__ __device__ static constexpr int len(int j) { return q + (j < r ? 1 : 0); }
+    __host__ __device__ static constexpr int klen(int j) {
+        return len(j) < kMaxKeyLen ? len(j) : kMaxKeyLen;
+    }
 };
 
+// Full compare of one candidate found through segment j; emits the hit if
+// it is within K after the N correction and j is its first exact segment.
+template <int K>
+__device__ __forceinline__ void check_candidate(const ScanParams &p, uint2 e, int j, uint32_t h20,
+                                                uint32_t l20, uint32_t n20g, uint32_t ne,
+                                                uint64_t slot, uint64_t pos, uint32_t gbeg) {
+    const uint32_t gh = e.x & 0xFFFFFu, gl = e.y & 0xFFFFFu;
+    const uint32_t m = (h20 ^ gh) | (l20 ^ gl);
+    const int cm = __popc(m);
+    if (cm > K) return;
+    bool first = true;
+#pragma unroll
+    for (int jj = 0; jj < K; ++jj)
+        if (jj < j)
+            first = first &&
+                    (((m >> Seg<K>::start(jj)) & ((1u << Seg<K>::klen(jj)) - 1u)) != 0u);
+    if (!first) return;
+    int mmf = cm;
+    if (n20g) {
+        const uint32_t eh = (ne & 2u) ? gh : ~gh;
+        const uint32_t el = (ne & 1u) ? gl : ~gl;
+        mmf = cm + __popc(n20g & eh & el);
+    }
+    if (mmf > K) return;
+    const uint32_t idx = (e.x >> 20) | ((e.y >> 20) << 12);
+    const uint32_t row = __ldg(&p.guides[gbeg + idx].row);
+    semit(((uint64_t)row << 39) | (slot << 38) | (pos << 6) | (uint64_t)mmf, p.keys, p.cap,
+          p.counter);
+}
+
+template <int K>
 __global__ void __launch_bounds__(kSeedThreads) scan_seed_kernel(ScanParams p, SeedArgs sa) {
+    constexpr int S = K + 1;
     extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t *sH = reinterpret_cast<uint32_t *>(smem);
-    uint32_t *sL = sH + kSeedTileWords;
-    uint32_t *sN = sL + kSeedTileWords;
-    uint16_t *sList = reinterpret_cast<uint16_t *>(sN + kSeedTileWords);
-    SeedFam *sFam = reinterpret_cast<SeedFam *>(sList + kSeedTileSites);
-    uint4 *sG = reinterpret_cast<uint4 *>(sFam + sa.n_fams);
-    uint32_t *sOff = reinterpret_cast<uint32_t *>(sG + sa.n_guides);
-    uint16_t *sLst = reinterpret_cast<uint16_t *>(sOff + sa.n_offsets);
-    __shared__ int sWarp[kSeedThreads / 32];
-    __shared__ int sTotal;
+    SeedFam *sFam = reinterpret_cast<SeedFam *>(smem);
+    uint2 *sEnt = reinterpret_cast<uint2 *>(sFam + sa.n_fams);
+    uint32_t *sOff = reinterpret_cast<uint32_t *>(sEnt + sa.n_lists);
+    unsigned char *slices =
+        smem + ((sizeof(SeedFam) * sa.n_fams + sizeof(uint2) * sa.n_lists +
+                 sizeof(uint32_t) * sa.n_offsets + 15) / 16 * 16);
     __shared__ unsigned long long sCand;
 
     const int t = threadIdx.x;
     const int lane = t & 31;
     const int warp = t >> 5;
-    const int K = p.max_mm;
+    unsigned char *slice = slices + warp * kWarpSliceBytes;
+    uint16_t *wList = reinterpret_cast<uint16_t *>(slice + kListOff);
+    uint4 *wRec = reinterpret_cast<uint4 *>(slice + kRecOff);
+    uint32_t *wQ = reinterpret_cast<uint32_t *>(slice + kQueueOff);
 
-    // stage the segment indexes and guide planes of every family once
     for (int i = t; i < sa.n_fams; i += kSeedThreads) sFam[i] = sa.fams[i];
-    for (int i = t; i < sa.n_guides; i += kSeedThreads) {
-        const GuideRec r = p.guides[i];
-        sG[i] = make_uint4(r.h, r.l, r.row, 0u);
-    }
+    for (int i = t; i < sa.n_lists; i += kSeedThreads) sEnt[i] = sa.entries[i];
     for (int i = t; i < sa.n_offsets; i += kSeedThreads) sOff[i] = sa.offsets[i];
-    for (int i = t; i < sa.n_lists; i += kSeedThreads) sLst[i] = sa.lists[i];
+    if (t == 0) sCand = 0;
+    __syncthreads();
 
-    for (int64_t tile = blockIdx.x; tile < p.tiles_total; tile += gridDim.x) {
-        const bool second = p.n_strands > 1 && tile >= p.strand[0].n_tiles;
-        const int64_t lt = second ? tile - p.strand[0].n_tiles : tile;
-        const uint32_t *H = second ? p.strand[1].H : p.strand[0].H;
-        const uint32_t *L = second ? p.strand[1].L : p.strand[0].L;
-        const uint32_t *N = second ? p.strand[1].N : p.strand[0].N;
+    const int64_t chunks0 = p.strand[0].n_tiles;
+    const int64_t n_chunks = p.tiles_total;
+    const int64_t stride = (int64_t)gridDim.x * kSeedWarps;
+    // Chunk c's words [c*64, c*64 + kChunkWords) of the three planes, copied
+    // into buffer b as 16-byte vectors (the planes are padded so that the copy
+    // never leaves them, and zero beyond total_bp).
+    auto issue = [&](int64_t c, int b) {
+        const bool second = c >= chunks0;
+        const int64_t w0 = (second ? c - chunks0 : c) * (kSeedChunkSites / 32);
+        const uint32_t *src[3] = {second ? p.strand[1].H : p.strand[0].H,
+                                  second ? p.strand[1].L : p.strand[0].L,
+                                  second ? p.strand[1].N : p.strand[0].N};
+        uint32_t *dst = reinterpret_cast<uint32_t *>(slice + b * kBufBytes);
+        for (int i = lane; i < 3 * kChunkVecs; i += 32) {
+            const int plane = i / kChunkVecs, v = i - plane * kChunkVecs;
+            cp_async16(dst + plane * kChunkWords + 4 * v, src[plane] + w0 + 4 * v);
+        }
+    };
+    uint32_t cand = 0;
+    const int64_t c_first = (int64_t)blockIdx.x * kSeedWarps + warp;
+    if (c_first < n_chunks) issue(c_first, 0);
+    cp_async_commit();
+    int buf = 0;
+    for (int64_t c = c_first; c < n_chunks; c += stride, buf ^= 1) {
+        if (c + stride < n_chunks) issue(c + stride, buf ^ 1);
+        cp_async_commit();
+        cp_async_wait<1>();  // this chunk's copies are done; the next one is in flight
+        __syncwarp();
+        const uint32_t *wH = reinterpret_cast<const uint32_t *>(slice + buf * kBufBytes);
+        const uint32_t *wL = wH + kChunkWords;
+        const uint32_t *wN = wL + kChunkWords;
+        const bool second = c >= chunks0;
+        const int64_t lc = second ? c - chunks0 : c;
         const int64_t total_bp = second ? p.strand[1].total_bp : p.strand[0].total_bp;
         const int has_n = second ? p.strand[1].has_n : p.strand[0].has_n;
         const uint32_t ne = (uint32_t)(second ? p.strand[1].n_encoded : p.strand[0].n_encoded);
         const uint64_t slot = (uint64_t)(second ? p.strand[1].slot : p.strand[0].slot);
-        const int64_t base = lt * kSeedTileSites;
-        const int64_t w0 = lt * (kSeedTileSites / 32);
+        const int64_t base = lc * kSeedChunkSites;
         const int64_t valid_end = total_bp - kSiteSpan;
-        const int64_t words_ok = (total_bp + 31) / 32 + 4;  // inside every plane allocation
-
-        __syncthreads();
-        for (int i = t; i < kSeedTileWords; i += kSeedThreads) {
-            const int64_t w = w0 + i;
-            const bool in = w < words_ok;
-            sH[i] = in ? H[w] : 0u;
-            sL[i] = in ? L[w] : 0u;
-            sN[i] = in ? N[w] : 0u;
-        }
-        uint32_t valid[kSeedWpt];
-#pragma unroll
-        for (int u = 0; u < kSeedWpt; ++u) {
-            const int64_t s0 = base + 32 * (kSeedWpt * t + u);
-            valid[u] = 0xFFFFFFFFu;
-            if (s0 >= valid_end) valid[u] = 0;
-            else if (valid_end - s0 < 32) valid[u] = (1u << (uint32_t)(valid_end - s0)) - 1u;
-        }
-        __syncthreads();
 
         for (int f = p.fam_begin; f < p.fam_end; ++f) {
             const FamilyDesc F = p.fams[f];
             const uint32_t pam_off = F.three_prime ? 20u : 0u;
             const uint32_t win_off = F.three_prime ? 0u : (uint32_t)F.plen;
-            if (t == 0) sCand = 0;
-
-            uint32_t pass[kSeedWpt];
+            uint32_t pass[kChunkRows];
             int cnt = 0;
 #pragma unroll
-            for (int u = 0; u < kSeedWpt; ++u) {
-                const int wi = kSeedWpt * t + u;
-                uint32_t ps = valid[u];
-                for (int k = 0; k < F.plen; ++k) {
-                    const uint32_t a = F.allowed[k] & 15u;
-                    if (a == 15u) continue;
-                    const uint32_t s = pam_off + (uint32_t)k;
-                    ps &= sallowed(sfshr(sH[wi], sH[wi + 1], s), sfshr(sL[wi], sL[wi + 1], s), a);
+            for (int u = 0; u < kChunkRows; ++u) {
+                const int wi = u * 32 + lane;
+                const int64_t s0 = base + 32 * wi;
+                uint32_t ps = 0xFFFFFFFFu;
+                if (s0 >= valid_end) ps = 0;
+                else if (valid_end - s0 < 32) ps = (1u << (uint32_t)(valid_end - s0)) - 1u;
+                const uint32_t h0 = wH[wi], h1 = wH[wi + 1], l0 = wL[wi], l1 = wL[wi + 1];
+#pragma unroll
+                for (int k = 0; k < kMaxPam; ++k) {
+                    if (k < F.plen) {
+                        const uint32_t a = F.allowed[k] & 15u;
+                        if (a != 15u) {
+                            const uint32_t s = pam_off + (uint32_t)k;
+                            ps &= sallowed(sfshr(h0, h1, s), sfshr(l0, l1, s), a);
+                        }
+                    }
                 }
                 pass[u] = ps;
                 cnt += __popc(ps);
@@ -143,185 +222,196 @@ __global__ void __launch_bounds__(kSeedThreads) scan_seed_kernel(ScanParams p, S
             int incl = cnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
                 if (lane >= o) incl += v;
             }
-            if (lane == 31) sWarp[warp] = incl;
-            __syncthreads();
-            if (warp == 0) {
-                int v = lane < kSeedThreads / 32 ? sWarp[lane] : 0;
-                int inc = v;
+            const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            int off = incl - cnt;
+#pragma unroll
+            for (int u = 0; u < kChunkRows; ++u) {
+                uint32_t m = pass[u];
+                while (m) {
+                    const int j = __ffs(m) - 1;
+                    m &= m - 1u;
+                    wList[off++] = (uint16_t)(32 * (u * 32 + lane) + j);
+                }
+            }
+            __syncwarp();
+            const SeedFam &SF = sFam[f];
+            const uint32_t gbeg = (uint32_t)F.gbeg, gfam = (uint32_t)(F.gend - F.gbeg);
+            for (int k0 = 0; k0 < total; k0 += 32) {
+                const int k = k0 + lane;
+                const bool has = k < total;
+                uint32_t s = 0, h20 = 0, l20 = 0, n20g = 0;
+                if (has) {
+                    s = wList[k];
+                    const uint32_t wo = s + win_off;
+                    const uint32_t wi = wo >> 5, b = wo & 31u;
+                    h20 = sfshr(wH[wi], wH[wi + 1], b) & 0xFFFFFu;
+                    l20 = sfshr(wL[wi], wL[wi + 1], b) & 0xFFFFFu;
+                    if (has_n) {
+                        const uint32_t n26 =
+                            sfshr(wN[s >> 5], wN[(s >> 5) + 1], s & 31u) & 0x3FFFFFFu;
+                        if (n26) n20g = sfshr(wN[wi], wN[wi + 1], b) & 0xFFFFFu;
+                    }
+                }
+                // bucket of each segment: entry start and count in one word
+                uint32_t ea[S], en[S];
+                uint32_t T = 0;
+#pragma unroll
+                for (int j = 0; j < S; ++j) {
+                    constexpr int dummy = 0;
+                    (void)dummy;
+                    const int st = Seg<K>::start(j), kl = Seg<K>::klen(j);
+                    const uint32_t km = (1u << kl) - 1u;
+                    const uint32_t code = (((h20 >> st) & km) << kl) | ((l20 >> st) & km);
+                    const uint32_t d = has ? sOff[SF.seg[j].off + code] : 0u;
+                    ea[j] = SF.list_off + (uint32_t)j * gfam + (d & 0xFFFFu);
+                    en[j] = d >> 16;
+                    T += en[j];
+                }
+                cand += T;
+                uint32_t tin = T;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    int u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-                    if (lane >= o) inc += u;
+                    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, tin, o);
+                    if (lane >= o) tin += v;
                 }
-                if (lane < kSeedThreads / 32) sWarp[lane] = inc - v;
-                if (lane == kSeedThreads / 32 - 1) sTotal = inc;
-            }
-            __syncthreads();
-            {
-                int off = sWarp[warp] + incl - cnt;
+                const uint32_t C = __shfl_sync(0xFFFFFFFFu, tin, 31);
+                if (C == 0) continue;
+                const uint64_t pos = (uint64_t)(base + s);
+                if (C <= (uint32_t)kQueueCap) {
+                    wRec[lane] = make_uint4(h20, l20, n20g, s);
+                    uint32_t qp = tin - T;
 #pragma unroll
-                for (int u = 0; u < kSeedWpt; ++u) {
-                    uint32_t m = pass[u];
-                    while (m) {
-                        const int j = __ffs(m) - 1;
-                        m &= m - 1u;
-                        sList[off++] = (uint16_t)(32 * (kSeedWpt * t + u) + j);
+                    for (int j = 0; j < S; ++j)
+                        for (uint32_t i = 0; i < en[j]; ++i)
+                            wQ[qp++] = (ea[j] + i) | ((uint32_t)j << 22) | ((uint32_t)lane << 27);
+                    __syncwarp();
+                    // two candidates per lane per iteration: both loads in flight
+                    for (uint32_t q = lane; q < C; q += 64) {
+                        const bool two = q + 32 < C;
+                        const uint32_t v0 = wQ[q];
+                        const uint32_t v1 = two ? wQ[q + 32] : v0;
+                        const uint4 r0 = wRec[v0 >> 27];
+                        const uint4 r1 = wRec[v1 >> 27];
+                        const uint2 e0 = sEnt[v0 & 0x3FFFFFu];
+                        const uint2 e1 = sEnt[v1 & 0x3FFFFFu];
+                        check_candidate<K>(p, e0, (int)((v0 >> 22) & 31u), r0.x, r0.y, r0.z, ne,
+                                           slot, (uint64_t)(base + r0.w), gbeg);
+                        if (two)
+                            check_candidate<K>(p, e1, (int)((v1 >> 22) & 31u), r1.x, r1.y, r1.z,
+                                               ne, slot, (uint64_t)(base + r1.w), gbeg);
                     }
+                    __syncwarp();
+                } else {
+#pragma unroll
+                    for (int j = 0; j < S; ++j)
+                        for (uint32_t i = 0; i < en[j]; ++i)
+                            check_candidate<K>(p, sEnt[ea[j] + i], j, h20, l20, n20g, ne, slot,
+                                               pos, gbeg);
                 }
             }
-            __syncthreads();
-            const int n_sites = sTotal;
-            const SeedFam &SF = sFam[f];
-            const int nseg = SF.nseg;
-            const uint32_t gfam = (uint32_t)(F.gend - F.gbeg);
-            uint32_t cand = 0;
-            for (int idx = t; idx < n_sites; idx += kSeedThreads) {
-                const uint32_t s = sList[idx];
-                const uint32_t wo = s + win_off;
-                const uint32_t wi = wo >> 5, b = wo & 31u;
-                const uint32_t h20 = sfshr(sH[wi], sH[wi + 1], b) & 0xFFFFFu;
-                const uint32_t l20 = sfshr(sL[wi], sL[wi + 1], b) & 0xFFFFFu;
-                for (int j = 0; j < nseg; ++j) {
-                    const SeedSeg sg = SF.seg[j];
-                    const uint32_t km = (1u << sg.klen) - 1u;
-                    const uint32_t code =
-                        (((h20 >> sg.start) & km) << sg.klen) | ((l20 >> sg.start) & km);
-                    const uint32_t qb = sOff[sg.off + code];
-                    const uint32_t qe = sOff[sg.off + code + 1];
-                    const uint16_t *Lj = sLst + SF.list_off + (uint32_t)j * gfam;
-                    cand += qe - qb;
-                    for (uint32_t q = qb; q < qe; ++q) {
-                        const uint4 G = sG[F.gbeg + Lj[q]];
-                        const uint32_t m = (h20 ^ G.x) | (l20 ^ G.y);
-                        const int cm = __popc(m);
-                        if (cm > K) continue;
-                        bool first = true;
-                        for (int jj = 0; jj < j; ++jj) {
-                            const SeedSeg s2 = SF.seg[jj];
-                            if (((m >> s2.start) & ((1u << s2.klen) - 1u)) == 0u) {
-                                first = false;
-                                break;
-                            }
-                        }
-                        if (!first) continue;
-                        int mmf = cm;
-                        if (has_n) {
-                            const uint32_t n26 =
-                                sfshr(sN[s >> 5], sN[(s >> 5) + 1], s & 31u) & 0x3FFFFFFu;
-                            if (n26) {
-                                const uint32_t n20 = sfshr(sN[wi], sN[wi + 1], b) & 0xFFFFFu;
-                                const uint32_t eh = (ne & 2u) ? G.x : ~G.x;
-                                const uint32_t el = (ne & 1u) ? G.y : ~G.y;
-                                mmf = cm + __popc(n20 & eh & el);
-                            }
-                        }
-                        if (mmf <= K) {
-                            const uint64_t pos = (uint64_t)(base + s);
-                            const uint64_t key = ((uint64_t)G.z << 39) | (slot << 38) |
-                                                 (pos << 6) | (uint64_t)mmf;
-                            semit(key, p.keys, p.cap, p.counter);
-                        }
-                    }
-                }
-            }
-            for (int o = 16; o > 0; o >>= 1) cand += __shfl_down_sync(0xFFFFFFFFu, cand, o);
-            if (lane == 0 && cand) atomicAdd(&sCand, (unsigned long long)cand);
-            __syncthreads();
-            if (t == 0 && sCand) atomicAdd(p.counter + 1, sCand);
+            __syncwarp();
         }
     }
-}
-
-size_t seed_static_smem_bytes() {
-    return sizeof(uint32_t) * 3 * kSeedTileWords + sizeof(uint16_t) * kSeedTileSites;
+    cp_async_wait<0>();
+    for (int o = 16; o > 0; o >>= 1) cand += __shfl_down_sync(0xFFFFFFFFu, cand, o);
+    if (lane == 0 && cand) atomicAdd(&sCand, (unsigned long long)cand);
+    __syncthreads();
+    if (t == 0 && sCand) atomicAdd(p.counter + 1, sCand);
 }
 
 size_t seed_smem_bytes(const SeedArgs &sa) {
-    size_t b = seed_static_smem_bytes();
-    b += sizeof(SeedFam) * sa.n_fams;
+    size_t b = sizeof(SeedFam) * sa.n_fams + sizeof(uint2) * sa.n_lists +
+               sizeof(uint32_t) * sa.n_offsets;
     b = (b + 15) / 16 * 16;
-    b += sizeof(uint4) * sa.n_guides + sizeof(uint32_t) * sa.n_offsets +
-         sizeof(uint16_t) * sa.n_lists;
-    return (b + 15) / 16 * 16;
+    return b + kSeedWarps * kWarpSliceBytes;
 }
 
-int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, cudaStream_t s) {
+template <int K>
+static int launch_k(const ScanParams &p, const SeedArgs &sa, int sm_count, cudaStream_t s) {
     const size_t smem = seed_smem_bytes(sa);
     static size_t configured = 0;
     if (smem > configured) {
-        BGO_CUDA(cudaFuncSetAttribute(scan_seed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+        BGO_CUDA(cudaFuncSetAttribute(scan_seed_kernel<K>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
     }
     int per_sm = 0;
-    BGO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_seed_kernel, kSeedThreads,
-                                                           smem));
+    BGO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_seed_kernel<K>,
+                                                           kSeedThreads, smem));
     if (per_sm < 1) per_sm = 1;
-    const int64_t grid = std::min<int64_t>(p.tiles_total, (int64_t)sm_count * per_sm);
-    scan_seed_kernel<<<(unsigned)grid, kSeedThreads, smem, s>>>(p, sa);
+    const int64_t blocks_needed = (p.tiles_total + kSeedWarps - 1) / kSeedWarps;
+    const int64_t grid = std::min<int64_t>(blocks_needed, (int64_t)sm_count * per_sm);
+    scan_seed_kernel<K><<<(unsigned)grid, kSeedThreads, smem, s>>>(p, sa);
     BGO_CUDA(cudaGetLastError());
     return BGO_OK;
 }
 
-// K + 1 segments as equal as possible, longer ones first; each bucket key is
-// the segment's first min(len, 6) bases.  False when the filter cannot apply.
-static bool seed_layout(int K, int *nseg, SeedSeg *segs) {
-    if (K < 0 || K + 1 > kGuideLen) return false;
-    const int S = K + 1;
-    const int q = kGuideLen / S, r = kGuideLen % S;
-    int start = 0;
-    for (int j = 0; j < S; ++j) {
-        const int len = q + (j < r ? 1 : 0);
-        segs[j].start = (uint8_t)start;
-        segs[j].len = (uint8_t)len;
-        segs[j].klen = (uint8_t)std::min(len, kMaxKeyLen);
-        segs[j].pad = 0;
-        segs[j].off = 0;
-        start += len;
+int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, cudaStream_t s) {
+    switch (p.max_mm) {
+        case 0: return launch_k<0>(p, sa, sm_count, s);
+        case 1: return launch_k<1>(p, sa, sm_count, s);
+        case 2: return launch_k<2>(p, sa, sm_count, s);
+        case 3: return launch_k<3>(p, sa, sm_count, s);
+        case 4: return launch_k<4>(p, sa, sm_count, s);
+        case 5: return launch_k<5>(p, sa, sm_count, s);
+        case 6: return launch_k<6>(p, sa, sm_count, s);
+        case 7: return launch_k<7>(p, sa, sm_count, s);
+        default:
+            set_error("segment index: max_mismatches outside 0..7");
+            return BGO_ERR_ARG;
     }
-    *nseg = S;
-    return true;
 }
 
+// The host index for K mismatches; false when the filter does not apply (K
+// outside 0..7, where K + 1 segments of 2-3 bases would not halve the
+// comparisons) or a family is too large for 16-bit bucket fields.  Bucket
+// descriptor = entry start within the segment's list | count << 16.
 bool build_seed_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
                       std::vector<SeedFam> &out_fams, std::vector<uint32_t> &offsets,
-                      std::vector<uint16_t> &lists) {
-    SeedSeg layout[kMaxSeg];
-    int S = 0;
-    if (!seed_layout(K, &S, layout)) return false;
-    double frac = 0;
-    for (int j = 0; j < S; ++j) frac += 1.0 / (double)(1u << (2 * layout[j].klen));
-    if (frac > 0.5) return false;  // the index would not halve the comparisons
+                      std::vector<uint2> &entries) {
+    if (K < 0 || K > kSeedMaxK) return false;
+    const int S = K + 1;
+    const int q = kGuideLen / S, r = kGuideLen % S;
     out_fams.assign((size_t)n_fams, SeedFam{});
     offsets.clear();
-    lists.clear();
+    entries.clear();
     for (int f = 0; f < n_fams; ++f) {
         const int G = fams[f].gend - fams[f].gbeg;
         if (G > 65535) return false;
         SeedFam &sf = out_fams[(size_t)f];
         sf.nseg = S;
-        sf.list_off = (uint32_t)lists.size();
-        lists.resize(lists.size() + (size_t)S * (size_t)G);
+        sf.list_off = (uint32_t)entries.size();
+        entries.resize(entries.size() + (size_t)S * (size_t)G);
+        if (entries.size() >= (1u << 22)) return false;
         for (int j = 0; j < S; ++j) {
-            SeedSeg sg = layout[j];
+            SeedSeg sg{};
+            sg.start = (uint8_t)(j * q + std::min(j, r));
+            sg.len = (uint8_t)(q + (j < r ? 1 : 0));
+            sg.klen = (uint8_t)std::min<int>(sg.len, kMaxKeyLen);
             sg.off = (uint32_t)offsets.size();
             const uint32_t nb = 1u << (2 * sg.klen);
             const uint32_t km = (1u << sg.klen) - 1u;
             std::vector<uint32_t> cnt(nb + 1, 0);
             std::vector<uint32_t> code((size_t)G);
             for (int i = 0; i < G; ++i) {
-                const GuideRec &r = recs[fams[f].gbeg + i];
-                code[(size_t)i] = (((r.h >> sg.start) & km) << sg.klen) | ((r.l >> sg.start) & km);
+                const GuideRec &rr = recs[fams[f].gbeg + i];
+                code[(size_t)i] = (((rr.h >> sg.start) & km) << sg.klen) | ((rr.l >> sg.start) & km);
                 cnt[code[(size_t)i] + 1]++;
             }
             for (uint32_t c = 0; c < nb; ++c) cnt[c + 1] += cnt[c];
-            offsets.insert(offsets.end(), cnt.begin(), cnt.end());
+            for (uint32_t c = 0; c < nb; ++c) offsets.push_back(cnt[c] | ((cnt[c + 1] - cnt[c]) << 16));
             std::vector<uint32_t> fill(cnt.begin(), cnt.end() - 1);
-            uint16_t *Lp = lists.data() + sf.list_off + (size_t)j * (size_t)G;
-            for (int i = 0; i < G; ++i) Lp[fill[code[(size_t)i]]++] = (uint16_t)i;
+            uint2 *E = entries.data() + sf.list_off + (size_t)j * (size_t)G;
+            for (int i = 0; i < G; ++i) {
+                const GuideRec &rr = recs[fams[f].gbeg + i];
+                uint2 e;
+                e.x = (rr.h & 0xFFFFFu) | (((uint32_t)i & 0xFFFu) << 20);
+                e.y = (rr.l & 0xFFFFFu) | (((uint32_t)i >> 12) << 20);
+                E[fill[code[(size_t)i]]++] = e;
+            }
             sf.seg[j] = sg;
         }
     }

@@ -149,22 +149,39 @@ def barrier(ws):
         dist.barrier()
 
 
-def plan_arrays(guides):
+MIXED_FAMILIES = (("NGG", 0.40), ("NG", 0.20), ("NNGRRT", 0.15), ("NNNRRT", 0.15),
+                  ("NRN", 0.10))
+
+
+def guide_pams(args, n):
+    """PAM of each guide: all NGG (plain configuration) or the mixed-family
+    split of the batched configuration."""
+    if args.config != "mixed":
+        return ["NGG"] * n
+    pams = []
+    for pam, frac in MIXED_FAMILIES:
+        pams += [pam] * int(round(frac * n))
+    return (pams + ["NGG"] * n)[:n]
+
+
+def plan_arrays(guides, pams=None):
     from beguidedoff_gb300.encoding import encode_dna, encode_guide_64bit
     from beguidedoff_gb300.pam import encode_pam_mask
 
     n = len(guides)
+    pams = pams or ["NGG"] * n
     gv = np.array([encode_guide_64bit(encode_dna(g)) for g in guides], dtype=np.uint64)
-    pm = np.tile(encode_pam_mask("NGG"), (n, 1))
-    return gv, pm, np.full(n, 3, dtype=np.uint8), np.ones(n, dtype=np.uint8)
+    pm = np.stack([encode_pam_mask(p) for p in pams]).astype(np.uint8)
+    pl = np.array([len(p) for p in pams], dtype=np.uint8)
+    return gv, pm, pl, np.ones(n, dtype=np.uint8)
 
 
-def cpu_scan_rate(genome, guides, max_mm, target_s, n_threads=0, budget_bp=None):
+def cpu_scan_rate(genome, guides, max_mm, target_s, n_threads=0, budget_bp=None, pams=None):
     """Oracle scan of both strands on a bounded prefix sample; returns
     (cmp/s, threads, sample description, seconds)."""
     from oracle import oracle as O
 
-    gv, pm, pl, p3 = plan_arrays(guides)
+    gv, pm, pl, p3 = plan_arrays(guides, pams)
     fwd_nm, rc_nm = O.prepare_n_masks(genome) if budget_bp is None else (None, None)
     nms = (genome.get("_nm_fwd_le"), genome.get("_nm_rc_le"))
     if nms[0] is not None:
@@ -195,21 +212,19 @@ def bench_reference(args, ws, rank):
     from beguidedoff_gb300 import _native
 
     lens, blocks, guides = make_workload(args.genome_bp, args.guides)
-    try:
-        genome = _native.synth_genome(7, lens, blocks, thresholds=(76, 128, 180),
-                                      device=int(os.environ.get("LOCAL_RANK", "0")))
-    except Exception:  # no GPU: generate nothing large on the host
-        raise
+    pams = guide_pams(args, len(guides))
+    genome = _native.synth_genome(7, lens, blocks, thresholds=(76, 128, 180),
+                                  device=int(os.environ.get("LOCAL_RANK", "0")))
     from beguidedoff_gb300.finder import prepare_n_masks
 
     genome["_nm_fwd_le"], genome["_nm_rc_le"] = prepare_n_masks(genome)
     per_step = max(1.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
-        cpu_scan_rate(genome, guides, args.max_mm, per_step / 4)
+        cpu_scan_rate(genome, guides, args.max_mm, per_step / 4, pams=pams)
     rates, sample, threads = [], "", 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r, threads, sample, _dt = cpu_scan_rate(genome, guides, args.max_mm, per_step)
+        r, threads, sample, _dt = cpu_scan_rate(genome, guides, args.max_mm, per_step, pams=pams)
         rates.append(r)
     wall = time.perf_counter() - t0
     value = statistics.median(rates)
@@ -229,11 +244,20 @@ def bench_reference(args, ws, rank):
 
 
 def workload_config(args, lens):
+    if args.config == "mixed":
+        name = (f"batched mixed-PAM scan: synthetic {int(lens.sum()) / 1e9:.2f} Gbp, "
+                f"24 chromosomes, GC 41%, 5% N blocks, {args.guides} random 20-nt guides "
+                f"(NGG 40% NG 20% NNGRRT 15% NNNRRT 15% NRN 10%), "
+                f"max_mismatches {args.max_mm}, both strands")
+        pam = "mixed"
+    else:
+        name = (f"human-scale plain scan: synthetic {int(lens.sum()) / 1e9:.2f} Gbp, "
+                f"24 chromosomes, GC 41%, 5% N blocks, {args.guides} random NGG guides, "
+                f"max_mismatches {args.max_mm}, both strands")
+        pam = "NGG"
     return {
-        "workload": (f"human-scale plain scan: synthetic {int(lens.sum()) / 1e9:.2f} Gbp, "
-                     f"24 chromosomes, GC 41%, 5% N blocks, {args.guides} random NGG guides, "
-                     f"max_mismatches {args.max_mm}, both strands"),
-        "genome_bp": int(lens.sum()), "guides": args.guides, "pam": "NGG",
+        "workload": name,
+        "genome_bp": int(lens.sum()), "guides": args.guides, "pam": pam,
         "max_mismatches": args.max_mm, "scan_mode": args.mode,
         "l2": "inputs larger than L2 (bit planes of both strands ~2.3 GB)",
     }
@@ -268,34 +292,58 @@ def bench_ours(args, ws, rank, local):
         hb = _native.HostBuffer((m.size,), np.uint8)
         hb.array[:] = m
         nm_pin.append(hb)
-    gv, pm, pl, p3 = plan_arrays(guides)
+    pams = guide_pams(args, len(guides))
+    gv, pm, pl, p3 = plan_arrays(guides, pams)
     plan = _native.Plan(f._engine, gv, pm, pl, p3)
     eng = f._engine
     comps = args.guides * 2 * (total - 26)
 
+    def timed(run_step, steps):
+        """CUDA-event time of `steps` steps on the launch stream (ms list, total ms)."""
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for k in range(steps):
+            run_step()
+            ev[k + 1].record(stream)
+        torch.cuda.synchronize()
+        return [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)], ev[0].elapsed_time(ev[-1])
+
+    # the plain form (one kernel per PAM family and strand) for comparison
+    plain = None
+    if args.config == "mixed" and args.mode != 0:
+        for _ in range(2):
+            eng.launch(plan, f._strands, [0, 3], args.max_mm, 0, sp)
+        ps, pt = timed(lambda: eng.launch(plan, f._strands, [0, 3], args.max_mm, 0, sp),
+                       max(2, args.steps // 2))
+        plain = {"mode": 0, "ms_per_step": pt / len(ps), "value": comps / (pt / len(ps) / 1e3),
+                 "hits_per_step": eng.hit_count(sp)}
+
     # -------- device-resident kernel timing (value) --------
+    graph = None
+    if args.mode == 2 and not args.no_graph:
+        graph = _native.Graph(eng, plan, f._strands, [0, 3], args.max_mm, 2)
+        step = lambda: graph.replay(sp)  # noqa: E731
+    else:
+        step = lambda: eng.launch(plan, f._strands, [0, 3], args.max_mm, args.mode, sp)  # noqa: E731
     for _ in range(args.warmup):
-        eng.launch(plan, f._strands, [0, 3], args.max_mm, args.mode, sp)
+        step()
     torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     n0 = eng.launch_count()
     clocks = ClockSampler(local).start()
     time.sleep(0.3)
     barrier(ws)
-    torch.cuda.synchronize()
-    ev[0].record(stream)
-    for k in range(args.steps):
-        eng.launch(plan, f._strands, [0, 3], args.max_mm, args.mode, sp)
-        ev[k + 1].record(stream)
-    torch.cuda.synchronize()
+    step_ms, total_ms = timed(step, args.steps)
     barrier(ws)
     clk = clocks.stop()
     launches = eng.launch_count() - n0
-    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
-    total_ms = ev[0].elapsed_time(ev[-1])
     t_max = dist_max(total_ms / 1e3, ws)
     hits = eng.hit_count(sp)
     pairs = eng.pairs_evaluated(sp)
+    if graph is not None:
+        graph.close()
+    if plain is not None:
+        plain["hits_equal"] = plain["hits_per_step"] == hits
 
     # -------- roofline: the compare loop is POPC-bound (1 POPC per pair) --------
     popc_peak = _native.probe_int_throughput(1, local)
@@ -313,7 +361,7 @@ def bench_ours(args, ws, rank, local):
     hbm_achieved = plane_bytes / (total_ms / 1e3 / args.steps) / 1e9
 
     # -------- end to end through the public API, genome uploaded each step --------
-    ginputs = [GuideInput(f"row_{i}", g, "NGG", "3prime", 4, 8, "ABE" if i % 2 == 0 else "CBE",
+    ginputs = [GuideInput(f"row_{i}", g, pams[i], "3prime", 4, 8, "ABE" if i % 2 == 0 else "CBE",
                           base_editor="ABE8e" if i % 2 == 0 else "TadCBEd")
                for i, g in enumerate(guides)]
     for s in f._strands:
@@ -345,7 +393,8 @@ def bench_ours(args, ws, rank, local):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         genome["_nm_fwd_le"], genome["_nm_rc_le"] = f._n_mask_fwd, f._n_mask_rc
-        rate, threads, sample, dt = cpu_scan_rate(genome, guides, args.max_mm, args.cpu_seconds)
+        rate, threads, sample, dt = cpu_scan_rate(genome, guides, args.max_mm, args.cpu_seconds,
+                                                  pams=pams)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": sample + f" ({dt:.1f} s, oracle/scan_oracle.c OpenMP)"}
 
@@ -381,6 +430,10 @@ def bench_ours(args, ws, rank, local):
                     "d2h_bytes_per_step": d2h, "s_per_step": e2e_s,
                     "rows": len(table), "launches": e2e_launches // args.steps},
             "gpu_launches": launches,
+            "graph": graph is not None,
+            "plain_form": plain,
+            "speedup_vs_plain": (plain["ms_per_step"] / (1e3 * t_max / args.steps)
+                                 if plain else None),
             "clocks": clk,
             "hits_per_step": hits,
             "step_ms": step_ms,
@@ -405,9 +458,17 @@ def main():
     ap.add_argument("--max-mm", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--config", default="plain", choices=["plain", "mixed"],
+                    help="plain: 100 NGG guides, <=4 mm; mixed: 400 mixed-PAM guides, <=5 mm")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.config == "mixed":
+        if "--guides" not in sys.argv:
+            args.guides = 400
+        if "--max-mm" not in sys.argv:
+            args.max_mm = 5
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         bench_reference(args, ws, rank)

@@ -126,6 +126,22 @@ int bgo_scan_collect(bgo_engine *engine, uint64_t *keys, int64_t capacity, int64
  * the work figure of the roofline. */
 int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
 
+/*
+ * The same scan as bgo_scan_launch, captured once into a CUDA graph and
+ * replayed by bgo_graph_launch (each replay resets the engine's counters and
+ * rescans; collect with bgo_scan_collect).  Everything that allocates or
+ * synchronises (the segment index, kernel attributes) happens at creation.
+ * The graph refers to the engine, plan and strands: keep them alive and
+ * unchanged while it exists; bgo_engine_reserve invalidates it.  No
+ * reference counterpart: the reference launches one kernel per 200 Mbp chunk.
+ */
+typedef struct bgo_graph bgo_graph;
+int bgo_graph_create(bgo_engine *engine, const bgo_plan *plan, const bgo_genome *const *strands,
+                     const int32_t *n_encoded, int32_t n_strands, int32_t max_mismatches,
+                     int32_t mode, bgo_graph **out);
+int bgo_graph_launch(bgo_graph *graph, void *stream);
+int bgo_graph_destroy(bgo_graph *graph);
+
 /* Grows the engine's device hit buffer to at least `n_hits` keys. */
 int bgo_engine_reserve(bgo_engine *engine, int64_t n_hits);
 

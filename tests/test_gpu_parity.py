@@ -153,6 +153,38 @@ def test_random_mixed_pam_keys_equal_oracle(seed):
         f.close()
 
 
+def test_graph_replay_equals_launch():
+    """A captured scan (bgo_graph_create / bgo_graph_launch) returns the same
+    keys as ordinary launches, on every replay, for the plain and indexed forms."""
+    genome, rng = _random_genome(21, [900_000, 500_000])
+    seqs, pams = [], []
+    for i in range(30):
+        s = "".join(rng.choice(list("ACGT"), 20))
+        _plant(genome, rng, s, MIXED_PAMS[i % 5], 4, 4)
+        seqs.append(s)
+        pams.append(MIXED_PAMS[i % 5])
+    f = beguidedoff(None, max_mismatches=5, genome_data=genome)
+    try:
+        exp = oracle_keys(genome, seqs, pams, 5)
+        gv = np.array([O.encode_guide(s) for s in seqs], dtype=np.uint64)
+        pm = np.zeros((len(seqs), 6), dtype=np.uint8)
+        for i, pam in enumerate(pams):
+            for j, ch in enumerate(pam):
+                pm[i, j] = IUPAC[ch]
+        pl = np.array([len(p) for p in pams], dtype=np.uint8)
+        plan = _native.Plan(f._engine, gv, pm, pl, np.ones(len(seqs), dtype=np.uint8))
+        for mode in (0, 2):
+            g = _native.Graph(f._engine, plan, f._strands, [0, 3], 5, mode)
+            for _ in range(2):
+                g.replay()
+                n, keys = f._engine.collect()
+                assert n == exp.size and np.array_equal(keys, exp), mode
+            g.close()
+        plan.close()
+    finally:
+        f.close()
+
+
 def test_large_genome_sampled_ranges_equal_oracle():
     """96 Mbp, 64 NGG guides: full GPU key set; the oracle re-scans four
     sampled 300 kbp ranges per strand and every planted site is found."""
