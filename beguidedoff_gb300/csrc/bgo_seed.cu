@@ -40,14 +40,15 @@ constexpr int kSeedWarps = kSeedThreads / 32;
 constexpr int kChunkRows = kSeedChunkSites / 1024;     // 32-position words per lane
 constexpr int kChunkWords = kSeedChunkSites / 32 + 4;  // 64 + halo, a multiple of 4 words
 constexpr int kChunkVecs = kChunkWords / 4;            // 16-byte copies per plane
-constexpr int kQueueCap = 512;                          // queued candidates per round
+constexpr int kQueueCap = 32 * (kSeedMaxK + 1);        // bucket ranges per round
 // per warp: two chunk buffers (H, L, N planes), the compacted list, the round's
-// position records and the candidate queue
+// position records and the bucket-range queue (word + count)
 constexpr size_t kBufBytes = 3 * kChunkWords * sizeof(uint32_t);
 constexpr size_t kListOff = 2 * kBufBytes;
 constexpr size_t kRecOff = (kListOff + kSeedChunkSites * sizeof(uint16_t) + 15) / 16 * 16;
 constexpr size_t kQueueOff = kRecOff + 32 * sizeof(uint4);
-constexpr size_t kWarpSliceBytes = (kQueueOff + kQueueCap * sizeof(uint32_t) + 15) / 16 * 16;
+constexpr size_t kCountOff = kQueueOff + kQueueCap * sizeof(uint32_t);
+constexpr size_t kWarpSliceBytes = (kCountOff + kQueueCap * sizeof(uint16_t) + 15) / 16 * 16;
 static_assert(kChunkWords % 4 == 0, "chunk copies are whole 16-byte vectors");
 static_assert(kBufBytes % 16 == 0, "chunk buffers stay 16-byte aligned");
 
@@ -127,7 +128,7 @@ __device__ __forceinline__ void check_candidate(const ScanParams &p, uint2 e, in
 }
 
 template <int K>
-__global__ void __launch_bounds__(kSeedThreads) scan_seed_kernel(ScanParams p, SeedArgs sa) {
+__global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p, SeedArgs sa) {
     constexpr int S = K + 1;
     extern __shared__ __align__(16) unsigned char smem[];
     SeedFam *sFam = reinterpret_cast<SeedFam *>(smem);
@@ -145,6 +146,7 @@ __global__ void __launch_bounds__(kSeedThreads) scan_seed_kernel(ScanParams p, S
     uint16_t *wList = reinterpret_cast<uint16_t *>(slice + kListOff);
     uint4 *wRec = reinterpret_cast<uint4 *>(slice + kRecOff);
     uint32_t *wQ = reinterpret_cast<uint32_t *>(slice + kQueueOff);
+    uint16_t *wCnt = reinterpret_cast<uint16_t *>(slice + kCountOff);
 
     for (int i = t; i < sa.n_fams; i += kSeedThreads) sFam[i] = sa.fams[i];
     for (int i = t; i < sa.n_lists; i += kSeedThreads) sEnt[i] = sa.entries[i];
@@ -237,8 +239,19 @@ __global__ void __launch_bounds__(kSeedThreads) scan_seed_kernel(ScanParams p, S
                 }
             }
             __syncwarp();
-            const SeedFam &SF = sFam[f];
-            const uint32_t gbeg = (uint32_t)F.gbeg, gfam = (uint32_t)(F.gend - F.gbeg);
+            // the family's bucket tables and entry bases, held in registers
+            // (shared-memory stores below would otherwise force reloads)
+            uint32_t seg_off[S], seg_ent[S];
+            {
+                const uint32_t list_off = sFam[f].list_off;
+                const uint32_t gf = (uint32_t)(F.gend - F.gbeg);
+#pragma unroll
+                for (int j = 0; j < S; ++j) {
+                    seg_off[j] = sFam[f].seg[j].off;
+                    seg_ent[j] = list_off + (uint32_t)j * gf;
+                }
+            }
+            const uint32_t gbeg = (uint32_t)F.gbeg;
             for (int k0 = 0; k0 < total; k0 += 32) {
                 const int k = k0 + lane;
                 const bool has = k < total;
@@ -260,57 +273,68 @@ __global__ void __launch_bounds__(kSeedThreads) scan_seed_kernel(ScanParams p, S
                 uint32_t T = 0;
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
-                    constexpr int dummy = 0;
-                    (void)dummy;
                     const int st = Seg<K>::start(j), kl = Seg<K>::klen(j);
                     const uint32_t km = (1u << kl) - 1u;
                     const uint32_t code = (((h20 >> st) & km) << kl) | ((l20 >> st) & km);
-                    const uint32_t d = has ? sOff[SF.seg[j].off + code] : 0u;
-                    ea[j] = SF.list_off + (uint32_t)j * gfam + (d & 0xFFFFu);
+                    const uint32_t d = has ? sOff[seg_off[j] + code] : 0u;
+                    ea[j] = seg_ent[j] + (d & 0xFFFFu);
                     en[j] = d >> 16;
                     T += en[j];
                 }
                 cand += T;
-                uint32_t tin = T;
+                // one queue slot per non-empty bucket: (entry start, segment,
+                // lane) and its count; at most K + 1 per lane, so 32 * (K + 1)
+                // slots always suffice
+                uint32_t R = 0;
+#pragma unroll
+                for (int j = 0; j < S; ++j) R += en[j] != 0u;
+                uint32_t rin = R;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, tin, o);
-                    if (lane >= o) tin += v;
+                    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, rin, o);
+                    if (lane >= o) rin += v;
                 }
-                const uint32_t C = __shfl_sync(0xFFFFFFFFu, tin, 31);
-                if (C == 0) continue;
-                const uint64_t pos = (uint64_t)(base + s);
-                if (C <= (uint32_t)kQueueCap) {
-                    wRec[lane] = make_uint4(h20, l20, n20g, s);
-                    uint32_t qp = tin - T;
+                const uint32_t RT = __shfl_sync(0xFFFFFFFFu, rin, 31);
+                if (RT == 0) continue;
+                wRec[lane] = make_uint4(h20, l20, n20g, s);
+                uint32_t qp = rin - R;
 #pragma unroll
-                    for (int j = 0; j < S; ++j)
-                        for (uint32_t i = 0; i < en[j]; ++i)
-                            wQ[qp++] = (ea[j] + i) | ((uint32_t)j << 22) | ((uint32_t)lane << 27);
-                    __syncwarp();
-                    // two candidates per lane per iteration: both loads in flight
-                    for (uint32_t q = lane; q < C; q += 64) {
-                        const bool two = q + 32 < C;
-                        const uint32_t v0 = wQ[q];
-                        const uint32_t v1 = two ? wQ[q + 32] : v0;
-                        const uint4 r0 = wRec[v0 >> 27];
-                        const uint4 r1 = wRec[v1 >> 27];
-                        const uint2 e0 = sEnt[v0 & 0x3FFFFFu];
-                        const uint2 e1 = sEnt[v1 & 0x3FFFFFu];
-                        check_candidate<K>(p, e0, (int)((v0 >> 22) & 31u), r0.x, r0.y, r0.z, ne,
-                                           slot, (uint64_t)(base + r0.w), gbeg);
-                        if (two)
-                            check_candidate<K>(p, e1, (int)((v1 >> 22) & 31u), r1.x, r1.y, r1.z,
-                                               ne, slot, (uint64_t)(base + r1.w), gbeg);
+                for (int j = 0; j < S; ++j) {
+                    if (en[j]) {
+                        wQ[qp] = ea[j] | ((uint32_t)j << 22) | ((uint32_t)lane << 27);
+                        wCnt[qp] = (uint16_t)en[j];
+                        ++qp;
                     }
-                    __syncwarp();
-                } else {
-#pragma unroll
-                    for (int j = 0; j < S; ++j)
-                        for (uint32_t i = 0; i < en[j]; ++i)
-                            check_candidate<K>(p, sEnt[ea[j] + i], j, h20, l20, n20g, ne, slot,
-                                               pos, gbeg);
                 }
+                __syncwarp();
+                for (uint32_t q = lane; q < RT; q += 32) {
+                    const uint32_t v = wQ[q];
+                    const uint32_t n = wCnt[q];
+                    const uint4 r = wRec[v >> 27];
+                    const uint32_t e0 = v & 0x3FFFFFu;
+                    const int j = (int)((v >> 22) & 31u);
+                    // four candidates per step: independent loads and counts,
+                    // then one test before the rare full check
+                    for (uint32_t i = 0; i < n; i += 4) {
+                        uint2 E[4];
+                        int cm[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const bool in = i + u < n;
+                            E[u] = in ? sEnt[e0 + i + u] : make_uint2(0u, 0u);
+                            const uint32_t m = (r.x ^ (E[u].x & 0xFFFFFu)) | (r.y ^ (E[u].y & 0xFFFFFu));
+                            cm[u] = in ? __popc(m) : 64;
+                        }
+                        if (min(min(cm[0], cm[1]), min(cm[2], cm[3])) <= K) {
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+                                if (cm[u] <= K)
+                                    check_candidate<K>(p, E[u], j, r.x, r.y, r.z, ne, slot,
+                                                       (uint64_t)(base + r.w), gbeg);
+                        }
+                    }
+                }
+                __syncwarp();
             }
             __syncwarp();
         }
