@@ -83,16 +83,26 @@ struct SeedSeg {
 struct SeedFam {
     int32_t nseg;
     uint32_t list_off;  // this family's lists: segment j at list_off + j * family size
-    uint32_t pad[2];
+    // PAM test program: n_tests constrained positions; test t checks the base
+    // at shift pam_shift[t] from the site.  pam_code[t]: bit 8 set = generic
+    // allowed-set test with nibble bits 0-3; else fixed bits: bit0 high-bit
+    // value, bit1 high-bit compared, bit2 low-bit value, bit3 low-bit compared
+    uint8_t n_tests;
+    uint8_t pam_shift[kMaxPam];
+    uint8_t pad0;
+    uint16_t pam_code[kMaxPam];
+    uint32_t pad1;
     SeedSeg seg[kMaxSeg];
 };
+static_assert(sizeof(SeedFam) % 16 == 0, "SeedFam arrays keep 16-byte alignment");
 
-// Bucket entry: guide planes h, l (20 bits each) with the family-local guide
-// index split over the top 12 bits of both words.
+// Bucket entries: guide planes h, l (20 bits each); entry_idx holds the
+// family-local guide index of each entry.
 struct SeedArgs {
     const SeedFam *fams;
     const uint32_t *offsets;  // per bucket: entry start | count << 16
     const uint2 *entries;
+    const uint16_t *entry_idx;
     int32_t n_fams, n_guides, n_offsets, n_lists;
 };
 
@@ -163,7 +173,7 @@ struct bgo_plan {
 namespace bgo {
 bool build_seed_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
                       std::vector<SeedFam> &out_fams, std::vector<uint32_t> &offsets,
-                      std::vector<uint2> &entries);
+                      std::vector<uint2> &entries, std::vector<uint16_t> &entry_idx);
 size_t seed_smem_bytes(const SeedArgs &sa);
 int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, cudaStream_t s);
 }  // namespace bgo

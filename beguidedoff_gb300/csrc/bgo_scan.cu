@@ -411,11 +411,15 @@ static int seed_prepare(bgo_plan *pl, int K, cudaStream_t s) {
     std::vector<SeedFam> sf;
     std::vector<uint32_t> offs;
     std::vector<uint2> ents;
-    if (!build_seed_index(pl->h_fams, pl->n_families, pl->h_guides, K, sf, offs, ents)) return 0;
+    std::vector<uint16_t> eidx;
+    if (!build_seed_index(pl->h_fams, pl->n_families, pl->h_guides, K, sf, offs, ents, eidx))
+        return 0;
     const size_t b_f = sizeof(SeedFam) * sf.size();
     const size_t b_e = sizeof(uint2) * ents.size();
     const size_t b_o = sizeof(uint32_t) * offs.size();
+    const size_t b_i = sizeof(uint16_t) * eidx.size();
     const size_t o_e = (b_f + 255) / 256 * 256, o_o = o_e + (b_e + 255) / 256 * 256;
+    const size_t o_i = o_o + (b_o + 255) / 256 * 256;
     SeedArgs sa{};
     sa.n_fams = (int32_t)sf.size();
     sa.n_guides = pl->n_active;
@@ -423,15 +427,18 @@ static int seed_prepare(bgo_plan *pl, int K, cudaStream_t s) {
     sa.n_lists = (int32_t)ents.size();
     // the whole index must fit in shared memory beside the warps' chunk slices
     if (seed_smem_bytes(sa) > 200 * 1024) return 0;
-    BGO_CUDA(cudaMalloc(&pl->d_seed, o_o + b_o + 16));
+    BGO_CUDA(cudaMalloc(&pl->d_seed, o_i + b_i + 16));
     BGO_CUDA(cudaMemcpyAsync(pl->d_seed, sf.data(), b_f, cudaMemcpyHostToDevice, s));
-    if (b_e)
+    if (b_e) {
         BGO_CUDA(cudaMemcpyAsync(pl->d_seed + o_e, ents.data(), b_e, cudaMemcpyHostToDevice, s));
+        BGO_CUDA(cudaMemcpyAsync(pl->d_seed + o_i, eidx.data(), b_i, cudaMemcpyHostToDevice, s));
+    }
     BGO_CUDA(cudaMemcpyAsync(pl->d_seed + o_o, offs.data(), b_o, cudaMemcpyHostToDevice, s));
     BGO_CUDA(cudaStreamSynchronize(s));
     sa.fams = reinterpret_cast<const SeedFam *>(pl->d_seed);
     sa.entries = reinterpret_cast<const uint2 *>(pl->d_seed + o_e);
     sa.offsets = reinterpret_cast<const uint32_t *>(pl->d_seed + o_o);
+    sa.entry_idx = reinterpret_cast<const uint16_t *>(pl->d_seed + o_i);
     pl->seed = sa;
     pl->seed_ok = 1;
     return 1;

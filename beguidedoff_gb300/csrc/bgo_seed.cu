@@ -14,19 +14,17 @@
 // also matches exactly, so each (position, guide) hit is emitted once.
 //
 // Layout.  Warps work independently (no CTA barrier after the start): each
-// warp takes chunks of kSeedChunkSites positions of one strand, copies the
-// chunk's H/L/N words (+2 halo words) to its own shared-memory slice, tests the
-// PAM of 32 positions per lane and word with funnel shifts and LOP3, and
-// compacts the passing positions into its own list with one warp scan.  Then,
-// 32 positions per round (one per lane), each lane looks up its K + 1 bucket
-// descriptors (one shared load each), the warp scans the candidate counts and
-// every lane writes its candidates (entry, segment, lane) into the warp's
-// queue; the whole warp then compares the queued candidates 32 at a time,
-// reading the owning position's window from the warp's record slots.  Rounds
-// whose candidates exceed the queue fall back to each lane walking its own
-// buckets.  The segment layout is a compile-time function of K, and every
-// bucket entry carries the guide's two 20-bit planes.  Hits are appended with
-// one atomicAdd per warp.
+// warp takes chunks of kSeedChunkSites positions of one strand and copies the
+// next chunk's H/L/N words with cp.async while it works on the current one
+// (double buffering).  Per PAM family it runs the family's compiled PAM test
+// on 32 positions per lane and word (funnel shifts + LOP3), compacts the
+// passing positions with one warp scan, then processes them 32 per round (one
+// per lane): the lane computes the K + 1 segment codes of its window, loads
+// each bucket descriptor and compares the bucket's first guide inline (all
+// lanes in step, predicated); buckets holding more guides leave the rest as a
+// range in the warp's queue, which the warp then works through.  The segment
+// layout is a compile-time function of K.  Hits are appended with one
+// atomicAdd per warp.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -67,10 +65,16 @@ __device__ __forceinline__ uint32_t sfshr(uint32_t lo, uint32_t hi, uint32_t s) 
     return __funnelshift_r(lo, hi, s);
 }
 
-__device__ __forceinline__ uint32_t sallowed(uint32_t h, uint32_t l, uint32_t a) {
-    const uint32_t m0 = 0u - (a & 1u), m1 = 0u - ((a >> 1) & 1u);
-    const uint32_t m2 = 0u - ((a >> 2) & 1u), m3 = 0u - ((a >> 3) & 1u);
-    return (~h & ~l & m0) | (~h & l & m1) | (h & ~l & m2) | (h & l & m3);
+// Positions (bits) whose base passes one compiled PAM test.
+__device__ __forceinline__ uint32_t pam_test(uint32_t h, uint32_t l, uint32_t code) {
+    if (code & 0x100u) {  // generic allowed set
+        const uint32_t m0 = 0u - (code & 1u), m1 = 0u - ((code >> 1) & 1u);
+        const uint32_t m2 = 0u - ((code >> 2) & 1u), m3 = 0u - ((code >> 3) & 1u);
+        return (~h & ~l & m0) | (~h & l & m1) | (h & ~l & m2) | (h & l & m3);
+    }
+    const uint32_t hv = 0u - (code & 1u), hc = 0u - ((code >> 1) & 1u);
+    const uint32_t lv = 0u - ((code >> 2) & 1u), lc = 0u - ((code >> 3) & 1u);
+    return ~(((h ^ hv) & hc) | ((l ^ lv) & lc));
 }
 
 __device__ __forceinline__ void semit(uint64_t key, uint64_t *keys, int64_t cap,
@@ -97,16 +101,13 @@ struct Seg {
     }
 };
 
-// Full compare of one candidate found through segment j; emits the hit if
-// it is within K after the N correction and j is its first exact segment.
+// The full check of a candidate whose raw count cm <= K, found through
+// segment j: emits the hit if j is its first exact segment and it stays
+// within K after the N correction.
 template <int K>
-__device__ __forceinline__ void check_candidate(const ScanParams &p, uint2 e, int j, uint32_t h20,
-                                                uint32_t l20, uint32_t n20g, uint32_t ne,
-                                                uint64_t slot, uint64_t pos, uint32_t gbeg) {
-    const uint32_t gh = e.x & 0xFFFFFu, gl = e.y & 0xFFFFFu;
-    const uint32_t m = (h20 ^ gh) | (l20 ^ gl);
-    const int cm = __popc(m);
-    if (cm > K) return;
+__device__ __noinline__ void finish_candidate(const ScanParams &p, uint32_t m, int cm, uint2 e,
+                                              uint32_t idx, int j, uint32_t n20g, uint32_t ne,
+                                              uint64_t slot, uint64_t pos, uint32_t gbeg) {
     bool first = true;
 #pragma unroll
     for (int jj = 0; jj < K; ++jj)
@@ -116,12 +117,11 @@ __device__ __forceinline__ void check_candidate(const ScanParams &p, uint2 e, in
     if (!first) return;
     int mmf = cm;
     if (n20g) {
-        const uint32_t eh = (ne & 2u) ? gh : ~gh;
-        const uint32_t el = (ne & 1u) ? gl : ~gl;
+        const uint32_t eh = (ne & 2u) ? e.x : ~e.x;
+        const uint32_t el = (ne & 1u) ? e.y : ~e.y;
         mmf = cm + __popc(n20g & eh & el);
     }
     if (mmf > K) return;
-    const uint32_t idx = (e.x >> 20) | ((e.y >> 20) << 12);
     const uint32_t row = __ldg(&p.guides[gbeg + idx].row);
     semit(((uint64_t)row << 39) | (slot << 38) | (pos << 6) | (uint64_t)mmf, p.keys, p.cap,
           p.counter);
@@ -134,9 +134,10 @@ __global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p
     SeedFam *sFam = reinterpret_cast<SeedFam *>(smem);
     uint2 *sEnt = reinterpret_cast<uint2 *>(sFam + sa.n_fams);
     uint32_t *sOff = reinterpret_cast<uint32_t *>(sEnt + sa.n_lists);
+    uint16_t *sIdx = reinterpret_cast<uint16_t *>(sOff + sa.n_offsets);
     unsigned char *slices =
         smem + ((sizeof(SeedFam) * sa.n_fams + sizeof(uint2) * sa.n_lists +
-                 sizeof(uint32_t) * sa.n_offsets + 15) / 16 * 16);
+                 sizeof(uint32_t) * sa.n_offsets + sizeof(uint16_t) * sa.n_lists + 15) / 16 * 16);
     __shared__ unsigned long long sCand;
 
     const int t = threadIdx.x;
@@ -149,7 +150,10 @@ __global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p
     uint16_t *wCnt = reinterpret_cast<uint16_t *>(slice + kCountOff);
 
     for (int i = t; i < sa.n_fams; i += kSeedThreads) sFam[i] = sa.fams[i];
-    for (int i = t; i < sa.n_lists; i += kSeedThreads) sEnt[i] = sa.entries[i];
+    for (int i = t; i < sa.n_lists; i += kSeedThreads) {
+        sEnt[i] = sa.entries[i];
+        sIdx[i] = sa.entry_idx[i];
+    }
     for (int i = t; i < sa.n_offsets; i += kSeedThreads) sOff[i] = sa.offsets[i];
     if (t == 0) sCand = 0;
     __syncthreads();
@@ -192,31 +196,32 @@ __global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p
         const uint32_t ne = (uint32_t)(second ? p.strand[1].n_encoded : p.strand[0].n_encoded);
         const uint64_t slot = (uint64_t)(second ? p.strand[1].slot : p.strand[0].slot);
         const int64_t base = lc * kSeedChunkSites;
-        const int64_t valid_end = total_bp - kSiteSpan;
+        // positions [0, lim) of this chunk are scanned (total_bp - 26 overall)
+        const int64_t lim64 = total_bp - kSiteSpan - base;
+        const int lim = lim64 > kSeedChunkSites ? kSeedChunkSites : (int)lim64;
 
         for (int f = p.fam_begin; f < p.fam_end; ++f) {
             const FamilyDesc F = p.fams[f];
-            const uint32_t pam_off = F.three_prime ? 20u : 0u;
             const uint32_t win_off = F.three_prime ? 0u : (uint32_t)F.plen;
+            const int n_tests = sFam[f].n_tests;
+            uint32_t tsh[kMaxPam], tcd[kMaxPam];
+#pragma unroll
+            for (int k = 0; k < kMaxPam; ++k) {
+                tsh[k] = sFam[f].pam_shift[k];
+                tcd[k] = sFam[f].pam_code[k];
+            }
             uint32_t pass[kChunkRows];
             int cnt = 0;
 #pragma unroll
             for (int u = 0; u < kChunkRows; ++u) {
                 const int wi = u * 32 + lane;
-                const int64_t s0 = base + 32 * wi;
-                uint32_t ps = 0xFFFFFFFFu;
-                if (s0 >= valid_end) ps = 0;
-                else if (valid_end - s0 < 32) ps = (1u << (uint32_t)(valid_end - s0)) - 1u;
+                const int rem = lim - 32 * wi;
+                uint32_t ps = rem >= 32 ? 0xFFFFFFFFu : (rem <= 0 ? 0u : (1u << rem) - 1u);
                 const uint32_t h0 = wH[wi], h1 = wH[wi + 1], l0 = wL[wi], l1 = wL[wi + 1];
 #pragma unroll
                 for (int k = 0; k < kMaxPam; ++k) {
-                    if (k < F.plen) {
-                        const uint32_t a = F.allowed[k] & 15u;
-                        if (a != 15u) {
-                            const uint32_t s = pam_off + (uint32_t)k;
-                            ps &= sallowed(sfshr(h0, h1, s), sfshr(l0, l1, s), a);
-                        }
-                    }
+                    if (k < n_tests)
+                        ps &= pam_test(sfshr(h0, h1, tsh[k]), sfshr(l0, l1, tsh[k]), tcd[k]);
                 }
                 pass[u] = ps;
                 cnt += __popc(ps);
@@ -240,7 +245,6 @@ __global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p
             }
             __syncwarp();
             // the family's bucket tables and entry bases, held in registers
-            // (shared-memory stores below would otherwise force reloads)
             uint32_t seg_off[S], seg_ent[S];
             {
                 const uint32_t list_off = sFam[f].list_off;
@@ -268,26 +272,35 @@ __global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p
                         if (n26) n20g = sfshr(wN[wi], wN[wi + 1], b) & 0xFFFFFu;
                     }
                 }
-                // bucket of each segment: entry start and count in one word
-                uint32_t ea[S], en[S];
-                uint32_t T = 0;
+                const uint64_t pos = (uint64_t)(base + s);
+                // per segment: bucket descriptor and an inline compare of the
+                // bucket's first guide; further guides stay as a range
+                uint32_t ra[S], rn[S];
+                uint32_t T = 0, R = 0;
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
                     const int st = Seg<K>::start(j), kl = Seg<K>::klen(j);
                     const uint32_t km = (1u << kl) - 1u;
                     const uint32_t code = (((h20 >> st) & km) << kl) | ((l20 >> st) & km);
                     const uint32_t d = has ? sOff[seg_off[j] + code] : 0u;
-                    ea[j] = seg_ent[j] + (d & 0xFFFFu);
-                    en[j] = d >> 16;
-                    T += en[j];
+                    const uint32_t n = d >> 16;
+                    const uint32_t e0 = seg_ent[j] + (d & 0xFFFFu);
+                    T += n;
+                    if (n) {
+                        const uint2 e = sEnt[e0];
+                        const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
+                        const int cm = __popc(m);
+                        if (cm <= K)
+                            finish_candidate<K>(p, m, cm, e, sIdx[e0], j, n20g, ne, slot, pos,
+                                                gbeg);
+                    }
+                    ra[j] = e0 + 1;
+                    rn[j] = n > 1u ? n - 1u : 0u;
+                    R += rn[j] != 0u;
                 }
                 cand += T;
-                // one queue slot per non-empty bucket: (entry start, segment,
-                // lane) and its count; at most K + 1 per lane, so 32 * (K + 1)
-                // slots always suffice
-                uint32_t R = 0;
-#pragma unroll
-                for (int j = 0; j < S; ++j) R += en[j] != 0u;
+                // buckets with more than one guide: ranges through the queue
+                if (!__any_sync(0xFFFFFFFFu, R != 0u)) continue;
                 uint32_t rin = R;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -295,14 +308,13 @@ __global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p
                     if (lane >= o) rin += v;
                 }
                 const uint32_t RT = __shfl_sync(0xFFFFFFFFu, rin, 31);
-                if (RT == 0) continue;
                 wRec[lane] = make_uint4(h20, l20, n20g, s);
                 uint32_t qp = rin - R;
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
-                    if (en[j]) {
-                        wQ[qp] = ea[j] | ((uint32_t)j << 22) | ((uint32_t)lane << 27);
-                        wCnt[qp] = (uint16_t)en[j];
+                    if (rn[j]) {
+                        wQ[qp] = ra[j] | ((uint32_t)j << 22) | ((uint32_t)lane << 27);
+                        wCnt[qp] = (uint16_t)rn[j];
                         ++qp;
                     }
                 }
@@ -313,25 +325,13 @@ __global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p
                     const uint4 r = wRec[v >> 27];
                     const uint32_t e0 = v & 0x3FFFFFu;
                     const int j = (int)((v >> 22) & 31u);
-                    // four candidates per step: independent loads and counts,
-                    // then one test before the rare full check
-                    for (uint32_t i = 0; i < n; i += 4) {
-                        uint2 E[4];
-                        int cm[4];
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            const bool in = i + u < n;
-                            E[u] = in ? sEnt[e0 + i + u] : make_uint2(0u, 0u);
-                            const uint32_t m = (r.x ^ (E[u].x & 0xFFFFFu)) | (r.y ^ (E[u].y & 0xFFFFFu));
-                            cm[u] = in ? __popc(m) : 64;
-                        }
-                        if (min(min(cm[0], cm[1]), min(cm[2], cm[3])) <= K) {
-#pragma unroll
-                            for (int u = 0; u < 4; ++u)
-                                if (cm[u] <= K)
-                                    check_candidate<K>(p, E[u], j, r.x, r.y, r.z, ne, slot,
-                                                       (uint64_t)(base + r.w), gbeg);
-                        }
+                    for (uint32_t i = 0; i < n; ++i) {
+                        const uint2 e = sEnt[e0 + i];
+                        const uint32_t m = (r.x ^ e.x) | (r.y ^ e.y);
+                        const int cm = __popc(m);
+                        if (cm <= K)
+                            finish_candidate<K>(p, m, cm, e, sIdx[e0 + i], j, r.z, ne, slot,
+                                                (uint64_t)(base + r.w), gbeg);
                     }
                 }
                 __syncwarp();
@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p
 
 size_t seed_smem_bytes(const SeedArgs &sa) {
     size_t b = sizeof(SeedFam) * sa.n_fams + sizeof(uint2) * sa.n_lists +
-               sizeof(uint32_t) * sa.n_offsets;
+               sizeof(uint32_t) * sa.n_offsets + sizeof(uint16_t) * sa.n_lists;
     b = (b + 15) / 16 * 16;
     return b + kSeedWarps * kWarpSliceBytes;
 }
@@ -389,26 +389,62 @@ int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, cu
     }
 }
 
+// PAM test program of a family: one test per constrained position (an N is
+// skipped).  Sets whose members share a fixed bit pattern of the 2-bit code
+// (single bases, R, Y, M, K) compare bits; S, W and the three-base codes use
+// the generic allowed-set select.
+static void pam_program(const FamilyDesc &F, SeedFam &sf) {
+    const uint32_t pam_off = F.three_prime ? 20u : 0u;
+    sf.n_tests = 0;
+    for (int k = 0; k < F.plen; ++k) {
+        const uint32_t a = F.allowed[k] & 15u;
+        if (a == 15u) continue;
+        int nb = 0, b0 = -1, b1 = -1;
+        for (int b = 0; b < 4; ++b)
+            if (a & (1u << b)) {
+                if (nb == 0) b0 = b;
+                else b1 = b;
+                ++nb;
+            }
+        uint16_t code;
+        if (nb == 1) {
+            code = (uint16_t)(((b0 >> 1) & 1) | 2 | ((b0 & 1) << 2) | 8);
+        } else if (nb == 2 && ((b0 & 1) == (b1 & 1)) && ((b0 >> 1) != (b1 >> 1))) {
+            code = (uint16_t)(((b0 & 1) << 2) | 8);  // low bit fixed (R, Y)
+        } else if (nb == 2 && ((b0 >> 1) == (b1 >> 1)) && ((b0 & 1) != (b1 & 1))) {
+            code = (uint16_t)(((b0 >> 1) & 1) | 2);  // high bit fixed (M, K)
+        } else {
+            code = (uint16_t)(0x100u | a);
+        }
+        sf.pam_shift[sf.n_tests] = (uint8_t)(pam_off + (uint32_t)k);
+        sf.pam_code[sf.n_tests] = code;
+        sf.n_tests++;
+    }
+}
+
 // The host index for K mismatches; false when the filter does not apply (K
 // outside 0..7, where K + 1 segments of 2-3 bases would not halve the
 // comparisons) or a family is too large for 16-bit bucket fields.  Bucket
 // descriptor = entry start within the segment's list | count << 16.
 bool build_seed_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
                       std::vector<SeedFam> &out_fams, std::vector<uint32_t> &offsets,
-                      std::vector<uint2> &entries) {
+                      std::vector<uint2> &entries, std::vector<uint16_t> &entry_idx) {
     if (K < 0 || K > kSeedMaxK) return false;
     const int S = K + 1;
     const int q = kGuideLen / S, r = kGuideLen % S;
     out_fams.assign((size_t)n_fams, SeedFam{});
     offsets.clear();
     entries.clear();
+    entry_idx.clear();
     for (int f = 0; f < n_fams; ++f) {
         const int G = fams[f].gend - fams[f].gbeg;
         if (G > 65535) return false;
         SeedFam &sf = out_fams[(size_t)f];
         sf.nseg = S;
+        pam_program(fams[f], sf);
         sf.list_off = (uint32_t)entries.size();
         entries.resize(entries.size() + (size_t)S * (size_t)G);
+        entry_idx.resize(entries.size());
         if (entries.size() >= (1u << 22)) return false;
         for (int j = 0; j < S; ++j) {
             SeedSeg sg{};
@@ -428,13 +464,12 @@ bool build_seed_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, 
             for (uint32_t c = 0; c < nb; ++c) cnt[c + 1] += cnt[c];
             for (uint32_t c = 0; c < nb; ++c) offsets.push_back(cnt[c] | ((cnt[c + 1] - cnt[c]) << 16));
             std::vector<uint32_t> fill(cnt.begin(), cnt.end() - 1);
-            uint2 *E = entries.data() + sf.list_off + (size_t)j * (size_t)G;
+            const size_t e_base = sf.list_off + (size_t)j * (size_t)G;
             for (int i = 0; i < G; ++i) {
                 const GuideRec &rr = recs[fams[f].gbeg + i];
-                uint2 e;
-                e.x = (rr.h & 0xFFFFFu) | (((uint32_t)i & 0xFFFu) << 20);
-                e.y = (rr.l & 0xFFFFFu) | (((uint32_t)i >> 12) << 20);
-                E[fill[code[(size_t)i]]++] = e;
+                const size_t at = e_base + fill[code[(size_t)i]]++;
+                entries[at] = make_uint2(rr.h & 0xFFFFFu, rr.l & 0xFFFFFu);
+                entry_idx[at] = (uint16_t)i;
             }
             sf.seg[j] = sg;
         }
