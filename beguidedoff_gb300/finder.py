@@ -91,7 +91,11 @@ class beguidedoff:
     def __init__(self, genome_path: str, max_mismatches: int = 4, scoring_method: str = "CCTOP",
                  device: Optional[str] = None, n_top_offtargets: int = 3,
                  results_per_guide: int = 10240, max_results_per_guide: Optional[int] = None,
-                 genome_data: Optional[dict] = None, scan_mode: int = 2):
+                 genome_data: Optional[dict] = None, scan_mode: int = 2,
+                 epilogue: str = "device"):
+        if epilogue not in ("device", "host"):
+            raise ValueError("epilogue must be 'device' or 'host'")
+        self.epilogue = epilogue
         self.genome_path = genome_path
         self.max_mismatches = max_mismatches
         if scoring_method.upper() != "CCTOP":
@@ -138,6 +142,7 @@ class beguidedoff:
         self.results_per_guide = results_per_guide
         self.max_results_per_guide = max_results_per_guide
         self.scan_mode = 1
+        self.epilogue = "host"
         self.device_index, self.device = -1, "none"
         self._engine, self._strands = None, []
         self._init_host(genome_data)
@@ -178,8 +183,7 @@ class beguidedoff:
             mapping[(g.guide_seq, g.pam, ci, lp, st)].append(g)
         return list(mapping), mapping
 
-    def _scan(self, plan_seqs: List[str], plan_pams: List[str]) -> np.ndarray:
-        """Device scan of both strands; sorted hit keys."""
+    def _plan(self, plan_seqs: List[str], plan_pams: List[str]):
         n = len(plan_seqs)
         gv = np.array([encode_guide_64bit(encode_dna(s)[:20]) for s in plan_seqs],
                       dtype=np.uint64)
@@ -188,13 +192,77 @@ class beguidedoff:
             pm[i] = encode_pam_mask(pam)
         pl = np.array([len(p) for p in plan_pams], dtype=np.uint8)
         p3 = np.ones(n, dtype=np.uint8)
-        plan = _native.Plan(self._engine, gv, pm, pl, p3)
+        return _native.Plan(self._engine, gv, pm, pl, p3)
+
+    def _scan(self, plan_seqs: List[str], plan_pams: List[str]) -> np.ndarray:
+        """Device scan of both strands; sorted hit keys."""
+        plan = self._plan(plan_seqs, plan_pams)
         try:
             ne = [0, 3][:len(self._strands)]
             return self._engine.scan(plan, self._strands, ne, self.max_mismatches,
                                      mode=self.scan_mode)
         finally:
             plan.close()
+
+    @staticmethod
+    def _window_cols(g) -> List[int]:
+        """Guide positions of the edit window as Python indexes a 20-nt string:
+        range(start - 1, end) below 20, negative indexes from the end."""
+        cols = [i if i >= 0 else 20 + i
+                for i in range(g.edit_window_start - 1, g.edit_window_end) if i < 20]
+        if any(c < 0 for c in cols):
+            raise IndexError("string index out of range")
+        return cols
+
+    def _search_device(self, keys, key_plan, plan_items, mapping, guides, return_all,
+                       count_score_threshold, log):
+        """Scan + device epilogue; the host only sorts each row's top-N
+        candidates.  Returns None when the host path must run instead
+        (a strand hit limit is reached, or an editor type is unknown)."""
+        from .scoring import score_ranks, threshold_rank
+
+        plan = self._plan([s for s, _ in plan_items], [p for _, p in plan_items])
+        try:
+            eng = self._engine
+            ne = [0, 3][:len(self._strands)]
+            eng.launch(plan, self._strands, ne, self.max_mismatches, self.scan_mode)
+            n = eng.hit_count()
+            if n > eng.info()["hit_capacity"]:
+                eng.reserve(n)
+                eng.launch(plan, self._strands, ne, self.max_mismatches, self.scan_mode)
+            rows, owners = [], []
+            for ki, key in enumerate(keys):
+                for g in mapping[key]:
+                    tb = TARGET_2BIT.get(g.editor_type)
+                    if tb is None:
+                        return None
+                    mask = 0
+                    for c in self._window_cols(g):
+                        mask |= 1 << c
+                    has_ot = key[2] is not None
+                    rows.append((key_plan[ki], mask, tb, key[2] if has_ot else -1,
+                                 key[3] if has_ot else 0, 0 if key[4] == "+" else 1, 0))
+                    owners.append(g.guide_id)
+            inputs = np.array(rows, dtype=_native.INPUT_ROW_DTYPE)
+            rank_table, _ = score_ranks()
+            below, groups, recs = eng.epilogue(
+                plan, self._strands, inputs, self.chrom_offsets, self.chrom_lengths,
+                rank_table, threshold_rank(count_score_threshold), self.n_top_offtargets,
+                return_all)
+        finally:
+            plan.close()
+        counts_k = groups[key_plan]
+        limit = self._limits(counts_k, keys, log)
+        if (counts_k.max(axis=1) > limit).any():
+            return None  # truncation needs the genome-order prefix of every strand
+        below_by_id: Dict[str, int] = defaultdict(int)
+        for gid, b in zip(owners, below.tolist()):
+            below_by_id[gid] += b
+        subset = np.unique(recs["key"])
+        return self._assemble(subset, keys, key_plan, plan_items, mapping, guides, return_all,
+                              count_score_threshold, log,
+                              precomputed=(limit, below_by_id if count_score_threshold is not None
+                                           else None))
 
     def _limits(self, counts2: np.ndarray, keys, log) -> np.ndarray:
         """Per scan key the per-strand number of hits kept, with the warnings
@@ -254,9 +322,14 @@ class beguidedoff:
         for i, k in enumerate(keys):
             key_plan[i] = plan_index.setdefault((k[0], k[1]), len(plan_index))
         plan_items = list(plan_index)
-        hit_keys = self._scan([s for s, _ in plan_items], [p for _, p in plan_items])
-        table = self._assemble(hit_keys, keys, key_plan, plan_items, mapping, guides, return_all,
-                               count_score_threshold, log)
+        table = None
+        if self.epilogue == "device":
+            table = self._search_device(keys, key_plan, plan_items, mapping, guides, return_all,
+                                        count_score_threshold, log)
+        if table is None:
+            hit_keys = self._scan([s for s, _ in plan_items], [p for _, p in plan_items])
+            table = self._assemble(hit_keys, keys, key_plan, plan_items, mapping, guides,
+                                   return_all, count_score_threshold, log)
         if output_file:
             table.to_csv(output_file, sep="\t", index=False)
             if verbose:
@@ -265,12 +338,19 @@ class beguidedoff:
 
     # ------------------------------------------------------------------
     def _assemble(self, hit_keys, keys, key_plan, plan_items, mapping, guides, return_all,
-                  count_score_threshold, log):
+                  count_score_threshold, log, precomputed=None):
+        """Output table from sorted hit keys.  ``precomputed`` = (per-key
+        strand limits, below-threshold counts by guide id or None) when the
+        keys are only the device epilogue's top-N candidates: no limit is
+        reached then, and the counts cover every hit."""
         row, slot, pos, mm = _native.split_keys(hit_keys)
         n_plan = len(plan_items)
-        counts2 = np.zeros((n_plan, 2), dtype=np.int64)
-        np.add.at(counts2, (row, slot), 1)
-        limit = self._limits(counts2[key_plan], keys, log)
+        if precomputed is None:
+            counts2 = np.zeros((n_plan, 2), dtype=np.int64)
+            np.add.at(counts2, (row, slot), 1)
+            limit = self._limits(counts2[key_plan], keys, log)
+        else:
+            limit = precomputed[0]
         offsets, lengths = self.chrom_offsets, self.chrom_lengths
         # keys are sorted by (row, strand, position): ranges per row, and the
         # rank of each hit inside its (row, strand) group
@@ -317,11 +397,14 @@ class beguidedoff:
         score = cctop_from_masks(mmask)
         include_non_editable = return_all
         below: Dict[str, int] = defaultdict(int)
+        if precomputed is not None and precomputed[1] is not None:
+            below = precomputed[1]
         per_input: Dict[str, List[np.ndarray]] = defaultdict(list)
         for ki, key in enumerate(keys):
             p_i = key_plan[ki]
             sel = np.arange(r_lo[p_i], r_hi[p_i])
-            sel = sel[rank[sel] < limit[ki]]
+            if precomputed is None:
+                sel = sel[rank[sel] < limit[ki]]
             if key[2] is not None and sel.size:
                 st_code = 0 if key[4] == "+" else 1
                 excl = ((ot_ci_hit[sel] == key[2]) & (ot_local_hit[sel] == key[3])
@@ -331,17 +414,13 @@ class beguidedoff:
                 tb = TARGET_2BIT.get(g.editor_type)
                 if tb is None:
                     raise ValueError(f"Unknown editor_type: {g.editor_type}")
-                # positions range(start - 1, end) below 20, indexed like a str
-                cols = [i if i >= 0 else 20 + i
-                        for i in range(g.edit_window_start - 1, g.edit_window_end) if i < 20]
-                if any(c < 0 for c in cols):
-                    raise IndexError("string index out of range")
+                cols = self._window_cols(g)
                 if cols and sel.size:
                     editable = (seq[sel][:, cols] == tb).any(axis=1)
                 else:
                     editable = np.zeros(sel.size, dtype=bool)
                 per_input[g.guide_id].append(sel if include_non_editable else sel[editable])
-                if count_score_threshold is not None:
+                if count_score_threshold is not None and precomputed is None:
                     below[g.guide_id] += int(
                         (editable & (score[sel] <= count_score_threshold)).sum())
         tables = []

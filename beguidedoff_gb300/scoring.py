@@ -22,6 +22,29 @@ def calculate_cctop_score(mismatch_positions: List[int]) -> float:
     return sum(1.2 ** pos for pos in mismatch_positions)
 
 
+_RANKS = None
+
+
+def score_ranks():
+    """(rank_table, distinct_scores): rank_table[mask] (uint32, 2^20 entries)
+    is the rank of mask's exact CCTOP score among ``distinct_scores``
+    (ascending float64), so comparing ranks orders hits exactly by score."""
+    global _RANKS
+    if _RANKS is None:
+        scores = cctop_from_masks(np.arange(1 << 20, dtype=np.int64))
+        distinct, inverse = np.unique(scores, return_inverse=True)
+        _RANKS = (np.ascontiguousarray(inverse.astype(np.uint32)), distinct)
+    return _RANKS
+
+
+def threshold_rank(threshold) -> int:
+    """Largest rank whose score is <= threshold (-1 if none or no threshold)."""
+    if threshold is None or threshold != threshold:  # None or NaN: nothing is <=
+        return -1
+    _, distinct = score_ranks()
+    return int(np.searchsorted(distinct, float(threshold), side="right")) - 1
+
+
 def cctop_from_masks(masks: np.ndarray, compensated: bool = COMPENSATED_SUM) -> np.ndarray:
     """Scores of 20-bit mismatch masks (bit p-1 = position p), equal to
     ``calculate_cctop_score`` of the listed positions."""

@@ -142,6 +142,48 @@ int bgo_graph_create(bgo_engine *engine, const bgo_plan *plan, const bgo_genome 
 int bgo_graph_launch(bgo_graph *graph, void *stream);
 int bgo_graph_destroy(bgo_graph *graph);
 
+/*
+ * Device epilogue of the engine's last scan: the per-hit work of the
+ * reference's host post-processing (beguidedoff/finder.py:193-244, :405-472,
+ * :545-566) without a per-hit host loop.  One bgo_input_row per input guide row
+ * (the reference's GuideInput after dedup to a plan row).
+ *   rank_table[mask]  rank of the exact CCTOP score of each 20-bit mismatch
+ *                     mask (bit p-1 = position p) among all distinct scores,
+ *                     ascending; 2^20 entries, built on the host;
+ *   threshold_rank    hits with rank <= it count as below the score threshold
+ *                     (-1: no threshold);
+ *   n_top, return_all the reference's top-N rule.
+ * Outputs: below[n_inputs] = the reference's n_offtargets_below_threshold;
+ * group_counts[2 * n_plan_rows] = hits per (plan row, strand slot); records =
+ * for every input row every included hit (editable, or any with return_all;
+ * on-target excluded) whose score rank is in the histogram bins up to the one
+ * holding its n_top-th hit - a superset of its top n_top that the caller
+ * sorts exactly.  *n_records is exact; nothing is copied if it exceeds
+ * capacity.
+ */
+typedef struct {
+    int32_t plan_row;     /* plan row of this input row's scan key             */
+    uint32_t window_mask; /* bit p-1: window position p is in the edit window  */
+    int32_t target_base;  /* 0 = A (ABE), 1 = C (CBE, CGE)                      */
+    int32_t ot_chrom;     /* on-target chromosome index, -1 = no exclusion      */
+    int64_t ot_local;     /* on-target local leftmost position (0-based)        */
+    int32_t ot_strand;    /* on-target strand slot: 0 '+', 1 '-'                */
+    int32_t pad;
+} bgo_input_row;
+
+typedef struct {
+    uint64_t key;      /* the hit key */
+    int32_t input_row; /* input row the hit is a candidate for */
+    uint32_t rank;     /* rank of its CCTOP score */
+} bgo_record;
+
+int bgo_epilogue_run(bgo_engine *engine, const bgo_plan *plan, const bgo_genome *const *strands,
+                     int32_t n_strands, const bgo_input_row *inputs, int32_t n_inputs,
+                     const int64_t *chrom_offsets, const int64_t *chrom_lengths, int32_t n_chroms,
+                     const uint32_t *rank_table, int32_t threshold_rank, int32_t n_top,
+                     int32_t return_all, int64_t *below, int64_t *group_counts,
+                     bgo_record *records, int64_t capacity, int64_t *n_records, void *stream);
+
 /* Grows the engine's device hit buffer to at least `n_hits` keys. */
 int bgo_engine_reserve(bgo_engine *engine, int64_t n_hits);
 

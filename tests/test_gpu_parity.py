@@ -24,16 +24,17 @@ def _lib():
     assert _native.device_count() >= 1
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("mode,epilogue", [(0, "device"), (1, "device"), (2, "device"),
+                                           (2, "host")])
 @pytest.mark.parametrize("name", FINDER_CASES)
-def test_finder_tables_match_reference(name, mode):
+def test_finder_tables_match_reference(name, mode, epilogue):
     case = Case(name)
     meta = case.meta
     f = beguidedoff(None, max_mismatches=meta["max_mismatches"],
                     n_top_offtargets=meta["n_top_offtargets"],
                     results_per_guide=meta["results_per_guide"],
                     max_results_per_guide=meta["max_results_per_guide"],
-                    genome_data=case.genome(), scan_mode=mode)
+                    genome_data=case.genome(), scan_mode=mode, epilogue=epilogue)
     try:
         for ri, run in enumerate(meta["runs"]):
             t = f.search(guides=case.guides(GuideInput), verbose=False, **run["kwargs"])
@@ -149,6 +150,57 @@ def test_random_mixed_pam_keys_equal_oracle(seed):
             f.scan_mode = mode
             got = f._scan(seqs, pams)
             assert got.size == exp.size and np.array_equal(got, exp), mode
+    finally:
+        f.close()
+
+
+@pytest.mark.parametrize("seed", [31, 32])
+def test_device_epilogue_tables_equal_host_assembly(seed):
+    """Device epilogue (exact score ranks, on-target exclusion, editable
+    window, below-threshold counts, per-row top-N candidates) against the host
+    assembly of the oracle's keys: identical tables, over input rows that share
+    scan keys with different editors and windows, on-targets taken from real
+    hits, tied scores, thresholds, return_all and several n_top values."""
+    genome, rng = _random_genome(seed, [600_000, 47, 350_000, 900_001])
+    seqs, pams = [], []
+    for i in range(24):
+        s = "".join(rng.choice(list("ACGT"), 20))
+        pam = MIXED_PAMS[i % len(MIXED_PAMS)]
+        _plant(genome, rng, s, pam, 12, 5)
+        seqs.append(s)
+        pams.append(pam)
+    seqs.append(seqs[0])   # a repeated (seq, pam) with its own on-target
+    pams.append(pams[0])
+    host = beguidedoff.host_only(genome, 5)
+    host._scan = lambda sq, pm: oracle_keys(genome, sq, pm, 5)
+    probe = host.search(guides=[GuideInput(f"p{i}", s, p, "3prime", 1, 20, "ABE")
+                                for i, (s, p) in enumerate(zip(seqs, pams))],
+                        return_all=True, verbose=False)
+    hits = table_rows(probe)
+    guides = []
+    editors = [("ABE", 4, 8), ("CBE", 3, 9), ("CGE", 1, 20), ("ABE", -3, 2), ("CBE", 18, 25)]
+    for i, (s, p) in enumerate(zip(seqs, pams)):
+        mine = [h for h in hits if h["guide_rna_sequence"] == s]
+        for j, (ed, a, b) in enumerate(editors[: 1 + i % len(editors)]):
+            ot = {}
+            if mine and (i + j) % 2 == 0:
+                h = mine[int(rng.integers(0, len(mine)))]
+                ot = dict(on_target_chrom=h["ot_chromosome"], on_target_pos=h["ot_position"],
+                          on_target_strand=h["ot_strand"])
+            guides.append(GuideInput(f"g{i % 20}", s, p, "3prime", a, b, ed,
+                                     base_editor=f"{ed}{j}", **ot))
+    f = beguidedoff(None, max_mismatches=5, genome_data=genome)
+    try:
+        for n_top in (1, 3, 50):
+            f.n_top_offtargets = host.n_top_offtargets = n_top
+            for kw in ({}, {"return_all": True}, {"count_score_threshold": 2.0},
+                       {"count_score_threshold": 20.0, "return_all": True},
+                       {"count_score_threshold": float("nan")}):
+                exp = table_rows(host.search(guides=guides, verbose=False, **kw))
+                got = table_rows(f.search(guides=guides, verbose=False, **kw))
+                ok, why = rows_equal(got, exp)
+                assert ok, f"n_top {n_top} {kw}: {why}"
+                assert len(exp) > 0
     finally:
         f.close()
 
