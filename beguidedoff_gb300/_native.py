@@ -26,7 +26,8 @@ EXPORTED = [
     "bgo_scan_launch", "bgo_scan_collect", "bgo_engine_reserve", "bgo_search_genome",
     "bgo_engine_info", "bgo_synth_genome", "bgo_probe_int_throughput", "bgo_scan_stats",
     "bgo_scan_noalloc", "bgo_graph_create", "bgo_graph_launch", "bgo_graph_destroy",
-    "bgo_epilogue_run",
+    "bgo_epilogue_run", "bgo_synth_genome_repeats", "bgo_engine_transfer",
+    "bgo_plan_set_tuning",
 ]
 
 INPUT_ROW_DTYPE = np.dtype([("plan_row", "<i4"), ("window_mask", "<u4"), ("target_base", "<i4"),
@@ -84,18 +85,32 @@ _SIGS = {
     "bgo_search_genome": ([_P, _P, _P, _P, _P, _P, _I32, _I32, _I32, _I64, _P, _P, _P, _P],
                           ctypes.c_int),
     "bgo_engine_info": ([_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)], ctypes.c_int),
+    "bgo_engine_transfer": ([_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)], ctypes.c_int),
+    "bgo_plan_set_tuning": ([_P, _P], ctypes.c_int),
     "bgo_synth_genome": ([ctypes.c_uint64, _P, _I32, _P, _P, _I64, _P, ctypes.c_int, _P, _P, _P],
                          ctypes.c_int),
     "bgo_probe_int_throughput": ([ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
                                  ctypes.c_int),
+    "bgo_synth_genome_repeats": ([ctypes.c_uint64, _P, _I32, _P, _P, _I64, _P, _P, _P,
+                                  ctypes.c_int, _P, _P, _P], ctypes.c_int),
 }
 
 
+class RepeatSpec(ctypes.Structure):
+    """bgo_repeat_spec."""
+    _fields_ = [("n_families", ctypes.c_int32), ("family_len", ctypes.c_int32),
+                ("n_copies", ctypes.c_int64), ("divergence_65536", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("seed", ctypes.c_uint64)]
+
+
 def synth_genome(seed, chrom_lengths, n_blocks=(), thresholds=(64, 128, 192), device=0,
-                 out=None):
+                 out=None, repeats=None):
     """Seeded synthetic genome dict in the reference .npz layout (device
     generator).  ``n_blocks`` = sorted disjoint (start, end) pairs; ``out`` may
-    supply preallocated (fwd, rc, n_mask) host arrays, e.g. pinned buffers."""
+    supply preallocated (fwd, rc, n_mask) host arrays, e.g. pinned buffers.
+    ``repeats`` = dict(n_families, family_len, n_copies, divergence, seed)
+    inserts repeat-family copies; the dict gains ``repeat_families`` (the
+    consensus sequences as strings)."""
     lens = np.ascontiguousarray(chrom_lengths, dtype=np.int64)
     total = int(lens.sum())
     nb = np.asarray(list(n_blocks), dtype=np.int64).reshape(-1, 2)
@@ -111,16 +126,32 @@ def synth_genome(seed, chrom_lengths, n_blocks=(), thresholds=(64, 128, 192), de
     else:
         fwd, rc, nm = out
         assert fwd.size >= n_words and rc.size >= n_words and nm.size >= n_bytes
-    check(lib().bgo_synth_genome(int(seed), ptr(lens), lens.size, ptr(starts), ptr(ends),
-                                 starts.size, ptr(th), int(device), fwd.ctypes.data,
-                                 rc.ctypes.data, nm.ctypes.data), "bgo_synth_genome")
+    fams = None
+    if repeats is None:
+        check(lib().bgo_synth_genome(int(seed), ptr(lens), lens.size, ptr(starts), ptr(ends),
+                                     starts.size, ptr(th), int(device), fwd.ctypes.data,
+                                     rc.ctypes.data, nm.ctypes.data), "bgo_synth_genome")
+    else:
+        spec = RepeatSpec(int(repeats["n_families"]), int(repeats["family_len"]),
+                          int(repeats["n_copies"]),
+                          int(round(float(repeats["divergence"]) * 65536)), 0,
+                          int(repeats.get("seed", seed)))
+        fams = np.zeros(spec.n_families * spec.family_len, dtype=np.uint8)
+        check(lib().bgo_synth_genome_repeats(
+            int(seed), ptr(lens), lens.size, ptr(starts), ptr(ends), starts.size, ptr(th),
+            ctypes.byref(spec), fams.ctypes.data, int(device), fwd.ctypes.data, rc.ctypes.data,
+            nm.ctypes.data), "bgo_synth_genome_repeats")
     offsets = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64)
-    return {
+    out = {
         "genome_forward": fwd[:n_words], "genome_rc": rc[:n_words],
         "chrom_names": np.array([f"chr{i + 1}" for i in range(lens.size)]),
         "chrom_offsets": offsets, "chrom_lengths": lens, "total_bp": total,
         "n_mask": nm[:n_bytes],
     }
+    if fams is not None:
+        out["repeat_families"] = ["".join("ACGT"[b] for b in r)
+                                  for r in fams.reshape(spec.n_families, spec.family_len)]
+    return out
 
 
 def probe_int_throughput(op, device=0):
@@ -235,6 +266,12 @@ class Strand:
             pass
 
 
+class Tuning(ctypes.Structure):
+    """bgo_tuning: launch parameters of scan modes 2 and 3 (0 = default)."""
+    _fields_ = [("chunk_sites", ctypes.c_int32), ("group_guides", ctypes.c_int32),
+                ("ctas_per_sm", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class Plan:
     """Guide rows grouped into PAM families on the device."""
 
@@ -260,6 +297,13 @@ class Plan:
         check(lib().bgo_plan_info(self.handle, ctypes.byref(nf), ctypes.byref(ng)),
               "bgo_plan_info")
         return {"n_families": nf.value, "n_guides": ng.value}
+
+    def set_tuning(self, chunk_sites=0, group_guides=0, ctas_per_sm=0):
+        """Launch parameters of scan modes 2 and 3 (see bgo_plan_set_tuning)."""
+        t = Tuning(int(chunk_sites), int(group_guides), int(ctas_per_sm), 0)
+        check(lib().bgo_plan_set_tuning(self.handle, ctypes.byref(t)), "bgo_plan_set_tuning")
+        self.tuning = {"chunk_sites": int(chunk_sites), "group_guides": int(group_guides),
+                       "ctas_per_sm": int(ctas_per_sm)}
 
     def close(self):
         if self.handle is not None and self.handle.value:
@@ -338,6 +382,13 @@ class Engine:
 
     def launch_count(self):
         return self.info()["launches"]
+
+    def transfer(self):
+        """Bytes copied by this engine's calls: {"h2d": ..., "d2h": ...}."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().bgo_engine_transfer(self.handle, ctypes.byref(a), ctypes.byref(b)),
+              "bgo_engine_transfer")
+        return {"h2d": a.value, "d2h": b.value}
 
     def epilogue(self, plan, strands, inputs, chrom_offsets, chrom_lengths, rank_table,
                  threshold_rank, n_top, return_all, stream=None):

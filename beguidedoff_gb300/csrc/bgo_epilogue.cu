@@ -23,6 +23,8 @@
 //      n_top per row; the records are a superset of every row's top n_top.
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include <algorithm>
 #include <new>
 #include <vector>
@@ -232,6 +234,7 @@ extern "C" int bgo_epilogue_run(bgo_engine *engine, const bgo_plan *plan,
         cudaStreamSynchronize(s);
         return (int64_t)n;
     }();
+    engine->d2h_bytes += 8;
     if (n_hits_host > engine->cap) {
         set_error("bgo_epilogue_run: the last scan overflowed the hit buffer; reserve and rescan");
         return BGO_ERR_STATE;
@@ -241,17 +244,33 @@ extern "C" int bgo_epilogue_run(bgo_engine *engine, const bgo_plan *plan,
     const size_t b_list = al(sizeof(int32_t) * list.size());
     const size_t b_in = al(sizeof(bgo_input_row) * (size_t)(n_inputs + 1));
     const size_t b_chr = al(sizeof(int64_t) * (size_t)n_chroms);
-    const size_t b_rank = al(sizeof(uint32_t) << 20);
     const size_t b_below = al(sizeof(unsigned long long) * (size_t)(n_inputs + 1));
     const size_t b_grp = al(sizeof(unsigned long long) * (size_t)(2 * n_rows + 2));
     const size_t b_hist = al(sizeof(unsigned int) * (size_t)(n_inputs + 1) * kRankBins);
     const size_t b_cut = al(sizeof(int32_t) * (size_t)(n_inputs + 1));
     const size_t b_out = al(sizeof(bgo_record) * (size_t)(capacity + 1));
     const size_t b_cnt = al(sizeof(unsigned long long));
-    const size_t total = b_rows + b_list + b_in + 2 * b_chr + b_rank + b_below + b_grp + b_hist +
-                         b_cut + b_out + b_cnt;
-    unsigned char *d = nullptr;
-    BGO_CUDA(cudaMalloc(&d, total));
+    const size_t total = b_rows + b_list + b_in + 2 * b_chr + b_below + b_grp + b_hist + b_cut +
+                         b_out + b_cnt;
+    // grow-only scratch and the rank table, kept by the engine across calls
+    if (total > engine->epi_bytes) {
+        if (engine->d_epi) cudaFree(engine->d_epi);
+        engine->d_epi = nullptr;
+        engine->epi_bytes = 0;
+        const size_t want = total + total / 4;
+        BGO_CUDA(cudaMalloc(&engine->d_epi, want));
+        engine->epi_bytes = want;
+    }
+    const size_t rank_n = (size_t)1 << 20;
+    if (!engine->d_rank) BGO_CUDA(cudaMalloc(&engine->d_rank, sizeof(uint32_t) * rank_n));
+    if (engine->h_rank.size() != rank_n ||
+        memcmp(engine->h_rank.data(), rank_table, sizeof(uint32_t) * rank_n) != 0) {
+        engine->h_rank.assign(rank_table, rank_table + rank_n);
+        BGO_CUDA(cudaMemcpyAsync(engine->d_rank, engine->h_rank.data(), sizeof(uint32_t) * rank_n,
+                                 cudaMemcpyHostToDevice, s));
+        engine->h2d_bytes += (int64_t)(sizeof(uint32_t) * rank_n);
+    }
+    unsigned char *d = engine->d_epi;
     size_t o = 0;
     auto take = [&](size_t b) {
         unsigned char *p = d + o;
@@ -264,7 +283,7 @@ extern "C" int bgo_epilogue_run(bgo_engine *engine, const bgo_plan *plan,
     bgo_input_row *d_in = (bgo_input_row *)take(b_in);
     int64_t *d_off = (int64_t *)take(b_chr);
     int64_t *d_len = (int64_t *)take(b_chr);
-    uint32_t *d_rank = (uint32_t *)take(b_rank);
+    uint32_t *d_rank = engine->d_rank;
     unsigned long long *d_below = (unsigned long long *)take(b_below);
     unsigned long long *d_grp = (unsigned long long *)take(b_grp);
     unsigned int *d_hist = (unsigned int *)take(b_hist);
@@ -286,7 +305,9 @@ extern "C" int bgo_epilogue_run(bgo_engine *engine, const bgo_plan *plan,
     }
     step(cudaMemcpyAsync(d_off, chrom_offsets, sizeof(int64_t) * n_chroms, cudaMemcpyHostToDevice, s));
     step(cudaMemcpyAsync(d_len, chrom_lengths, sizeof(int64_t) * n_chroms, cudaMemcpyHostToDevice, s));
-    step(cudaMemcpyAsync(d_rank, rank_table, sizeof(uint32_t) << 20, cudaMemcpyHostToDevice, s));
+    engine->h2d_bytes += (int64_t)(sizeof(RowInfo) * rows.size() +
+                                   (sizeof(int32_t) + sizeof(bgo_input_row)) * (size_t)n_inputs +
+                                   2 * sizeof(int64_t) * (size_t)n_chroms);
     step(cudaMemsetAsync(d_below, 0, b_below + b_grp + b_hist, s));
     step(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long), s));
     e.keys = engine->d_keys;
@@ -337,12 +358,14 @@ extern "C" int bgo_epilogue_run(bgo_engine *engine, const bgo_plan *plan,
     step(cudaMemcpyAsync(tmp_g.data(), d_grp, sizeof(unsigned long long) * (size_t)(2 * n_rows + 2),
                          cudaMemcpyDeviceToHost, s));
     step(cudaStreamSynchronize(s));
+    engine->d2h_bytes += (int64_t)(sizeof(n_out) + sizeof(unsigned long long) *
+                                                       (size_t)(n_inputs + 1 + 2 * n_rows + 2));
     if (ce == cudaSuccess && (int64_t)n_out <= capacity && n_out > 0) {
         step(cudaMemcpyAsync(records, d_out, sizeof(bgo_record) * (size_t)n_out,
                              cudaMemcpyDeviceToHost, s));
         step(cudaStreamSynchronize(s));
+        engine->d2h_bytes += (int64_t)(sizeof(bgo_record) * n_out);
     }
-    cudaFree(d);
     if (ce != cudaSuccess) return cuda_fail(ce, "bgo_epilogue_run");
     for (int32_t i = 0; i < n_inputs; ++i) below[i] = (int64_t)tmp_b[(size_t)i];
     for (int32_t i = 0; i < 2 * n_rows; ++i) group_counts[i] = (int64_t)tmp_g[(size_t)i];

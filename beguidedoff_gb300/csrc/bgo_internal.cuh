@@ -106,9 +106,48 @@ struct SeedArgs {
     int32_t n_fams, n_guides, n_offsets, n_lists;
 };
 
-inline int64_t seed_tiles_for(int64_t total_bp) {
+// Segment-mask scan (scan mode 3): the segment index stored as guide bitmasks.
+// Each family is cut into groups of at most kMaskGroupMax guides; for group g,
+// segment j and key code c the table holds the bitmask of the group's guides
+// whose segment-j key equals c, in 1, 2 or 4 words.
+constexpr int kMaskThreads = 256;
+constexpr int kMaskMaxK = 7;
+constexpr int kMaskKeyLen = 4;     // bases per segment key: <= 256 codes
+constexpr int kMaskGroupMax = 128;
+
+struct MaskFam {
+    uint16_t g0, g1;  // groups [g0, g1)
+    uint8_t n_tests;  // PAM test program, as SeedFam
+    uint8_t pam_shift[kMaxPam];
+    uint8_t pad0;
+    uint16_t pam_code[kMaxPam];
+    uint32_t pad1[2];
+};
+static_assert(sizeof(MaskFam) % 16 == 0, "MaskFam arrays keep 16-byte alignment");
+
+struct MaskGroup {
+    uint32_t table_off;  // first table word (a multiple of the width)
+    uint32_t guide_off;  // first entry of the group in the guide-plane array
+    uint32_t gbeg;       // first row of the group in the family-sorted guide table
+    uint16_t n;          // guides in the group
+    uint8_t words;       // mask width in 32-bit words: 1, 2 or 4
+    uint8_t pad;
+};
+static_assert(sizeof(MaskGroup) == 16, "MaskGroup is one 16-byte load");
+
+struct MaskArgs {
+    const MaskFam *fams;
+    const MaskGroup *groups;
+    const uint32_t *table;
+    const uint2 *guides;  // (h, l) 20-bit planes per group entry
+    int32_t n_fams, n_groups, table_words, n_guides;
+    int32_t chunk_sites;  // positions per warp chunk: 1024 or 2048
+    int32_t pad;
+};
+
+inline int64_t seed_tiles_for(int64_t total_bp, int chunk_sites = kSeedChunkSites) {
     int64_t valid = total_bp - kSiteSpan;
-    return valid > 0 ? (valid + kSeedChunkSites - 1) / kSeedChunkSites : 0;
+    return valid > 0 ? (valid + chunk_sites - 1) / chunk_sites : 0;
 }
 
 void set_error(const std::string &msg);
@@ -168,6 +207,13 @@ struct bgo_plan {
     int seed_ok;              // 0: the filter does not apply to this K
     unsigned char *d_seed;    // device block: families | offsets | lists
     bgo::SeedArgs seed;
+    // segment-mask index for one (max_mismatches, group size) pair
+    int mask_k;               // -1000 = not built
+    int mask_group;           // guides per group it was built with
+    int mask_ok;
+    unsigned char *d_mask;    // device block: families | groups | table | guides
+    bgo::MaskArgs mask;
+    bgo_tuning tuning;        // launch parameters chosen by the caller (zeros = defaults)
 };
 
 namespace bgo {
@@ -176,6 +222,14 @@ bool build_seed_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, 
                       std::vector<uint2> &entries, std::vector<uint16_t> &entry_idx);
 size_t seed_smem_bytes(const SeedArgs &sa);
 int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, cudaStream_t s);
+void pam_program(const FamilyDesc &F, SeedFam &sf);
+bool build_mask_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
+                      int group_max, std::vector<MaskFam> &out_fams,
+                      std::vector<MaskGroup> &groups, std::vector<uint32_t> &table,
+                      std::vector<uint2> &guides);
+size_t mask_smem_bytes(const MaskArgs &ma);
+int launch_mask_kernel(const ScanParams &p, const MaskArgs &ma, int sm_count, int ctas_per_sm,
+                       cudaStream_t s);
 }  // namespace bgo
 
 struct bgo_engine {
@@ -186,4 +240,13 @@ struct bgo_engine {
     int64_t launches;
     int launched;
     int sm_count;
+    // epilogue: grow-only scratch and the device copy of the score-rank table
+    unsigned char *d_epi = nullptr;
+    size_t epi_bytes = 0;
+    uint32_t *d_rank = nullptr;
+    std::vector<uint32_t> h_rank;   // host copy of what d_rank holds
+    // bytes copied host -> device and device -> host by engine calls
+    int64_t h2d_bytes = 0, d2h_bytes = 0;
+    // bumped whenever d_keys / cap change (captured graphs re-capture then)
+    uint64_t keys_gen = 0;
 };

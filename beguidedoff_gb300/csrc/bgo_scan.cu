@@ -244,6 +244,8 @@ extern "C" int bgo_engine_destroy(bgo_engine *e) {
     cudaSetDevice(e->device);
     if (e->d_keys) cudaFree(e->d_keys);
     if (e->d_counter) cudaFree(e->d_counter);
+    if (e->d_epi) cudaFree(e->d_epi);
+    if (e->d_rank) cudaFree(e->d_rank);
     delete e;
     return BGO_OK;
 }
@@ -255,9 +257,19 @@ extern "C" int bgo_engine_reserve(bgo_engine *e, int64_t n_hits) {
     int64_t cap = std::max<int64_t>(n_hits, e->cap * 2);
     uint64_t *p = nullptr;
     BGO_CUDA(cudaMalloc(&p, (size_t)cap * sizeof(uint64_t)));
+    // the old buffer may still be written by work in flight on any stream
+    BGO_CUDA(cudaDeviceSynchronize());
     if (e->d_keys) cudaFree(e->d_keys);
     e->d_keys = p;
     e->cap = cap;
+    e->keys_gen++;
+    return BGO_OK;
+}
+
+extern "C" int bgo_engine_transfer(const bgo_engine *e, int64_t *h2d_bytes, int64_t *d2h_bytes) {
+    if (!e || !h2d_bytes || !d2h_bytes) return BGO_ERR_ARG;
+    *h2d_bytes = e->h2d_bytes;
+    *d2h_bytes = e->d2h_bytes;
     return BGO_OK;
 }
 
@@ -339,6 +351,11 @@ extern "C" int bgo_plan_create(bgo_engine *engine, const uint64_t *guide_encoded
     pl->h_fams = new (std::nothrow) FamilyDesc[fams.size() + 1];
     pl->h_guides = new (std::nothrow) GuideRec[recs.size() + 1];
     pl->seed_k = -1000;
+    pl->mask_k = -1000;
+    pl->mask_group = 0;
+    pl->mask_ok = 0;
+    pl->d_mask = nullptr;
+    pl->tuning = bgo_tuning{};
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = (pl->h_fams && pl->h_guides) ? cudaSuccess : cudaErrorMemoryAllocation;
     if (e == cudaSuccess) {
@@ -358,6 +375,7 @@ extern "C" int bgo_plan_create(bgo_engine *engine, const uint64_t *guide_encoded
         bgo_plan_destroy(pl);
         return cuda_fail(e, "bgo_plan_create");
     }
+    engine->h2d_bytes += (int64_t)(sizeof(FamilyDesc) * fams.size() + sizeof(GuideRec) * recs.size());
     *out = pl;
     return BGO_OK;
 }
@@ -370,7 +388,22 @@ extern "C" int bgo_plan_destroy(bgo_plan *pl) {
     delete[] pl->h_fams;
     delete[] pl->h_guides;
     if (pl->d_seed) cudaFree(pl->d_seed);
+    if (pl->d_mask) cudaFree(pl->d_mask);
     delete pl;
+    return BGO_OK;
+}
+
+extern "C" int bgo_plan_set_tuning(bgo_plan *pl, const bgo_tuning *t) {
+    if (!pl || !t) return BGO_ERR_ARG;
+    if ((t->chunk_sites != 0 && t->chunk_sites != 1024 && t->chunk_sites != 2048) ||
+        (t->group_guides != 0 && t->group_guides != 32 && t->group_guides != 64 &&
+         t->group_guides != 128) ||
+        t->ctas_per_sm < 0) {
+        set_error("bgo_plan_set_tuning: chunk_sites 1024|2048, group_guides 32|64|128, "
+                  "ctas_per_sm >= 0");
+        return BGO_ERR_ARG;
+    }
+    pl->tuning = *t;
     return BGO_OK;
 }
 
@@ -399,7 +432,7 @@ static void fill_strand(StrandDesc &d, const bgo_genome *g, int32_t n_encoded, i
 // Builds (once per max_mismatches value) and uploads the plan's segment
 // index.  Returns 1 when the index applies, 0 when the scan must compare every
 // guide (mode 1), or a negative BGO_ERR_*.
-static int seed_prepare(bgo_plan *pl, int K, cudaStream_t s) {
+static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s) {
     if (pl->seed_k == K) return pl->seed_ok;
     if (pl->d_seed) {
         BGO_CUDA(cudaStreamSynchronize(s));
@@ -435,6 +468,7 @@ static int seed_prepare(bgo_plan *pl, int K, cudaStream_t s) {
     }
     BGO_CUDA(cudaMemcpyAsync(pl->d_seed + o_o, offs.data(), b_o, cudaMemcpyHostToDevice, s));
     BGO_CUDA(cudaStreamSynchronize(s));
+    engine->h2d_bytes += (int64_t)(b_f + b_e + b_i + b_o);
     sa.fams = reinterpret_cast<const SeedFam *>(pl->d_seed);
     sa.entries = reinterpret_cast<const uint2 *>(pl->d_seed + o_e);
     sa.offsets = reinterpret_cast<const uint32_t *>(pl->d_seed + o_o);
@@ -444,12 +478,66 @@ static int seed_prepare(bgo_plan *pl, int K, cudaStream_t s) {
     return 1;
 }
 
+// Builds (once per (max_mismatches, group size)) and uploads the plan's
+// segment-mask index.  Returns 1 when it applies, 0 when the scan must compare
+// every guide (mode 1), or a negative BGO_ERR_*.
+static int mask_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s) {
+    const int group = pl->tuning.group_guides ? pl->tuning.group_guides : kMaskGroupMax;
+    const int chunk = pl->tuning.chunk_sites ? pl->tuning.chunk_sites : 2048;
+    if (pl->mask_k == K && pl->mask_group == group) {
+        pl->mask.chunk_sites = chunk;
+        if (pl->mask_ok && mask_smem_bytes(pl->mask) > 220 * 1024) return 0;
+        return pl->mask_ok;
+    }
+    if (pl->d_mask) {
+        BGO_CUDA(cudaStreamSynchronize(s));
+        cudaFree(pl->d_mask);
+        pl->d_mask = nullptr;
+    }
+    pl->mask_k = K;
+    pl->mask_group = group;
+    pl->mask_ok = 0;
+    std::vector<MaskFam> mf;
+    std::vector<MaskGroup> groups;
+    std::vector<uint32_t> table;
+    std::vector<uint2> gd;
+    if (!build_mask_index(pl->h_fams, pl->n_families, pl->h_guides, K, group, mf, groups, table,
+                          gd))
+        return 0;
+    const size_t b_f = sizeof(MaskFam) * mf.size(), b_g = sizeof(MaskGroup) * groups.size();
+    const size_t b_t = sizeof(uint32_t) * table.size(), b_d = sizeof(uint2) * gd.size();
+    auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t o_g = al(b_f), o_t = o_g + al(b_g), o_d = o_t + al(b_t);
+    MaskArgs ma{};
+    ma.n_fams = (int32_t)mf.size();
+    ma.n_groups = (int32_t)groups.size();
+    ma.table_words = (int32_t)table.size();
+    ma.n_guides = (int32_t)gd.size();
+    ma.chunk_sites = chunk;
+    // the whole index must fit in shared memory beside the warps' chunk slices
+    if (mask_smem_bytes(ma) > 220 * 1024) return 0;
+    BGO_CUDA(cudaMalloc(&pl->d_mask, o_d + b_d + 16));
+    BGO_CUDA(cudaMemcpyAsync(pl->d_mask, mf.data(), b_f, cudaMemcpyHostToDevice, s));
+    if (b_g) BGO_CUDA(cudaMemcpyAsync(pl->d_mask + o_g, groups.data(), b_g, cudaMemcpyHostToDevice, s));
+    if (b_t) BGO_CUDA(cudaMemcpyAsync(pl->d_mask + o_t, table.data(), b_t, cudaMemcpyHostToDevice, s));
+    if (b_d) BGO_CUDA(cudaMemcpyAsync(pl->d_mask + o_d, gd.data(), b_d, cudaMemcpyHostToDevice, s));
+    BGO_CUDA(cudaStreamSynchronize(s));
+    engine->h2d_bytes += (int64_t)(b_f + b_g + b_t + b_d);
+    ma.fams = reinterpret_cast<const MaskFam *>(pl->d_mask);
+    ma.groups = reinterpret_cast<const MaskGroup *>(pl->d_mask + o_g);
+    ma.table = reinterpret_cast<const uint32_t *>(pl->d_mask + o_t);
+    ma.guides = reinterpret_cast<const uint2 *>(pl->d_mask + o_d);
+    pl->mask = ma;
+    pl->mask_ok = 1;
+    return 1;
+}
+
 extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
                                const bgo_genome *const *strands, const int32_t *n_encoded,
                                int32_t n_strands, int32_t max_mismatches, int32_t mode,
                                void *stream) {
     if (!engine || !plan || !strands || !n_encoded || n_strands < 1 || n_strands > 2 ||
-        mode < 0 || mode > 2) {
+        mode < 0 || mode > 3) {
         set_error("bgo_scan_launch: invalid argument");
         return BGO_ERR_ARG;
     }
@@ -493,10 +581,27 @@ extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
             }
         }
     }
-    const int seeded = mode == 2 ? seed_prepare(const_cast<bgo_plan *>(plan), max_mismatches, s) : 0;
+    bgo_plan *mpl = const_cast<bgo_plan *>(plan);
+    const int seeded = mode == 2 ? seed_prepare(engine, mpl, max_mismatches, s) : 0;
     if (seeded < 0) return seeded;
+    const int masked = mode == 3 ? mask_prepare(engine, mpl, max_mismatches, s) : 0;
+    if (masked < 0) return masked;
     if (mode == 0) {
         // launched above
+    } else if (masked == 1) {
+        const int chunk = plan->mask.chunk_sites;
+        for (int i = 0; i < n_strands; ++i) {
+            fill_strand(p.strand[i], strands[i], n_encoded[i], i);
+            p.strand[i].n_tiles = seed_tiles_for(strands[i]->total_bp, chunk);
+        }
+        p.n_strands = n_strands;
+        p.tiles_total = p.strand[0].n_tiles + (n_strands > 1 ? p.strand[1].n_tiles : 0);
+        if (p.tiles_total == 0) return BGO_OK;
+        p.fam_begin = 0;
+        p.fam_end = plan->n_families;
+        const int rc = launch_mask_kernel(p, plan->mask, engine->sm_count, plan->tuning.ctas_per_sm, s);
+        if (rc != BGO_OK) return rc;
+        engine->launches++;
     } else if (seeded == 1) {
         for (int i = 0; i < n_strands; ++i) {
             fill_strand(p.strand[i], strands[i], n_encoded[i], i);
@@ -530,7 +635,40 @@ struct bgo_graph {
     bgo_engine *engine;
     cudaGraphExec_t exec;
     int64_t launches_per_replay;
+    // what the graph scans, for a re-capture after the hit buffer moved
+    const bgo_plan *plan;
+    std::vector<const bgo_genome *> strands;
+    std::vector<int32_t> n_encoded;
+    int32_t max_mismatches, mode;
+    uint64_t keys_gen;
 };
+
+// Captures one bgo_scan_launch on a private stream (nothing runs).
+static int capture_scan(bgo_graph *g, cudaGraphExec_t *out) {
+    bgo_engine *engine = g->engine;
+    cudaStream_t cs = nullptr;
+    BGO_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const int64_t before = engine->launches;
+    int rc = BGO_OK;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        rc = bgo_scan_launch(engine, g->plan, g->strands.data(), g->n_encoded.data(),
+                             (int32_t)g->strands.size(), g->max_mismatches, g->mode, cs);
+        cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+        if (e2 != cudaSuccess && rc == BGO_OK) e = e2;
+    }
+    if (rc == BGO_OK && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    g->launches_per_replay = engine->launches - before;
+    engine->launches = before;  // the capture itself ran nothing
+    if (rc != BGO_OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "bgo_graph capture");
+    *out = exec;
+    return BGO_OK;
+}
 
 extern "C" int bgo_graph_create(bgo_engine *engine, const bgo_plan *plan,
                                 const bgo_genome *const *strands, const int32_t *n_encoded,
@@ -538,39 +676,37 @@ extern "C" int bgo_graph_create(bgo_engine *engine, const bgo_plan *plan,
                                 bgo_graph **out) {
     if (!out) return BGO_ERR_ARG;
     *out = nullptr;
-    if (!engine) return BGO_ERR_ARG;
+    if (!engine || !plan || !strands || !n_encoded || n_strands < 1 || n_strands > 2)
+        return BGO_ERR_ARG;
     BGO_CUDA(cudaSetDevice(engine->device));
-    cudaStream_t cs = nullptr;
-    BGO_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     // one ordinary launch first: builds the segment index, sets kernel
     // attributes and validates the arguments outside the capture
-    int rc = bgo_scan_launch(engine, plan, strands, n_encoded, n_strands, max_mismatches, mode, cs);
-    cudaError_t e = rc == BGO_OK ? cudaStreamSynchronize(cs) : cudaSuccess;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    const int64_t before = engine->launches;
-    if (rc == BGO_OK && e == cudaSuccess)
-        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (rc == BGO_OK && e == cudaSuccess) {
-        rc = bgo_scan_launch(engine, plan, strands, n_encoded, n_strands, max_mismatches, mode, cs);
-        cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
-        if (e2 != cudaSuccess && rc == BGO_OK) e = e2;
+    {
+        cudaStream_t cs = nullptr;
+        BGO_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        int rc = bgo_scan_launch(engine, plan, strands, n_encoded, n_strands, max_mismatches,
+                                 mode, cs);
+        cudaError_t e = rc == BGO_OK ? cudaStreamSynchronize(cs) : cudaSuccess;
+        cudaStreamDestroy(cs);
+        if (rc != BGO_OK) return rc;
+        if (e != cudaSuccess) return cuda_fail(e, "bgo_graph_create");
     }
-    if (rc == BGO_OK && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
-    if (graph) cudaGraphDestroy(graph);
-    cudaStreamDestroy(cs);
-    if (rc != BGO_OK) return rc;
-    if (e != cudaSuccess) return cuda_fail(e, "bgo_graph_create");
     bgo_graph *g = new (std::nothrow) bgo_graph();
-    if (!g) {
-        cudaGraphExecDestroy(exec);
-        return BGO_ERR_OOM;
-    }
+    if (!g) return BGO_ERR_OOM;
     g->device = engine->device;
     g->engine = engine;
-    g->exec = exec;
-    g->launches_per_replay = engine->launches - before;
-    engine->launches = before;  // the capture itself ran nothing
+    g->plan = plan;
+    g->strands.assign(strands, strands + n_strands);
+    g->n_encoded.assign(n_encoded, n_encoded + n_strands);
+    g->max_mismatches = max_mismatches;
+    g->mode = mode;
+    g->keys_gen = engine->keys_gen;
+    g->exec = nullptr;
+    const int rc = capture_scan(g, &g->exec);
+    if (rc != BGO_OK) {
+        delete g;
+        return rc;
+    }
     *out = g;
     return BGO_OK;
 }
@@ -578,6 +714,16 @@ extern "C" int bgo_graph_create(bgo_engine *engine, const bgo_plan *plan,
 extern "C" int bgo_graph_launch(bgo_graph *g, void *stream) {
     if (!g) return BGO_ERR_ARG;
     BGO_CUDA(cudaSetDevice(g->device));
+    if (g->keys_gen != g->engine->keys_gen) {
+        // the hit buffer moved (bgo_engine_reserve): the captured kernels
+        // would write to the freed buffer, so capture again
+        cudaGraphExec_t exec = nullptr;
+        const int rc = capture_scan(g, &exec);
+        if (rc != BGO_OK) return rc;
+        cudaGraphExecDestroy(g->exec);
+        g->exec = exec;
+        g->keys_gen = g->engine->keys_gen;
+    }
     BGO_CUDA(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
     g->engine->launched = 1;
     g->engine->launches += g->launches_per_replay;
@@ -605,10 +751,12 @@ extern "C" int bgo_scan_collect(bgo_engine *engine, uint64_t *keys, int64_t capa
     BGO_CUDA(cudaMemcpyAsync(&n, engine->d_counter, sizeof(n), cudaMemcpyDeviceToHost, s));
     BGO_CUDA(cudaStreamSynchronize(s));
     *n_hits = (int64_t)n;
+    engine->d2h_bytes += (int64_t)sizeof(n);
     if (keys && (int64_t)n <= capacity && (int64_t)n <= engine->cap && n > 0) {
         BGO_CUDA(cudaMemcpyAsync(keys, engine->d_keys, (size_t)n * sizeof(uint64_t),
                                  cudaMemcpyDeviceToHost, s));
         BGO_CUDA(cudaStreamSynchronize(s));
+        engine->d2h_bytes += (int64_t)(n * sizeof(uint64_t));
         std::sort(keys, keys + n);
     }
     return BGO_OK;

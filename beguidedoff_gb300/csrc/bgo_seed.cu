@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "bgo_device.cuh"
 #include "bgo_internal.cuh"
 
 namespace bgo {
@@ -49,45 +50,6 @@ constexpr size_t kCountOff = kQueueOff + kQueueCap * sizeof(uint32_t);
 constexpr size_t kWarpSliceBytes = (kCountOff + kQueueCap * sizeof(uint16_t) + 15) / 16 * 16;
 static_assert(kChunkWords % 4 == 0, "chunk copies are whole 16-byte vectors");
 static_assert(kBufBytes % 16 == 0, "chunk buffers stay 16-byte aligned");
-
-// Asynchronous 16-byte global -> shared copy (completes at cp.async.wait_group).
-__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
-    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
-}
-
-__device__ __forceinline__ uint32_t sfshr(uint32_t lo, uint32_t hi, uint32_t s) {
-    return __funnelshift_r(lo, hi, s);
-}
-
-// Positions (bits) whose base passes one compiled PAM test.
-__device__ __forceinline__ uint32_t pam_test(uint32_t h, uint32_t l, uint32_t code) {
-    if (code & 0x100u) {  // generic allowed set
-        const uint32_t m0 = 0u - (code & 1u), m1 = 0u - ((code >> 1) & 1u);
-        const uint32_t m2 = 0u - ((code >> 2) & 1u), m3 = 0u - ((code >> 3) & 1u);
-        return (~h & ~l & m0) | (~h & l & m1) | (h & ~l & m2) | (h & l & m3);
-    }
-    const uint32_t hv = 0u - (code & 1u), hc = 0u - ((code >> 1) & 1u);
-    const uint32_t lv = 0u - ((code >> 2) & 1u), lc = 0u - ((code >> 3) & 1u);
-    return ~(((h ^ hv) & hc) | ((l ^ lv) & lc));
-}
-
-__device__ __forceinline__ void semit(uint64_t key, uint64_t *keys, int64_t cap,
-                                      unsigned long long *counter) {
-    unsigned act = __activemask();
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(act) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(act));
-    base = __shfl_sync(act, base, leader);
-    unsigned long long slot = base + (unsigned long long)__popc(act & ((1u << lane) - 1u));
-    if (slot < (unsigned long long)cap) keys[slot] = key;
-}
 
 // The K + 1 segments: start and key length (the segment's first <= 6 bases).
 template <int K>
@@ -167,13 +129,12 @@ __global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p
     auto issue = [&](int64_t c, int b) {
         const bool second = c >= chunks0;
         const int64_t w0 = (second ? c - chunks0 : c) * (kSeedChunkSites / 32);
-        const uint32_t *src[3] = {second ? p.strand[1].H : p.strand[0].H,
-                                  second ? p.strand[1].L : p.strand[0].L,
-                                  second ? p.strand[1].N : p.strand[0].N};
+        const StrandDesc &sd = second ? p.strand[1] : p.strand[0];
         uint32_t *dst = reinterpret_cast<uint32_t *>(slice + b * kBufBytes);
         for (int i = lane; i < 3 * kChunkVecs; i += 32) {
             const int plane = i / kChunkVecs, v = i - plane * kChunkVecs;
-            cp_async16(dst + plane * kChunkWords + 4 * v, src[plane] + w0 + 4 * v);
+            const uint32_t *src = plane == 0 ? sd.H : plane == 1 ? sd.L : sd.N;
+            cp_async16(dst + plane * kChunkWords + 4 * v, src + w0 + 4 * v);
         }
     };
     uint32_t cand = 0;
@@ -393,7 +354,7 @@ int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, cu
 // skipped).  Sets whose members share a fixed bit pattern of the 2-bit code
 // (single bases, R, Y, M, K) compare bits; S, W and the three-base codes use
 // the generic allowed-set select.
-static void pam_program(const FamilyDesc &F, SeedFam &sf) {
+void pam_program(const FamilyDesc &F, SeedFam &sf) {
     const uint32_t pam_off = F.three_prime ? 20u : 0u;
     sf.n_tests = 0;
     for (int k = 0; k < F.plen; ++k) {

@@ -9,15 +9,22 @@
 // mask).  The reverse-complement array is built per chromosome in the same
 // chromosome order as the reference converter (beguidedoff/genome_converter.py
 // :66-71), so the output is exactly what convert() writes for the same FASTA.
+//
+// Repeat families (optional): the genome is cut into n_copies equal regions and
+// region r holds one copy of family f_r at a seeded offset, in a seeded
+// orientation, with each base substituted (to one of the three other bases)
+// with the given probability.  Copies never overlap, and a copy base is again
+// a pure function of its position, so both strands stay consistent.
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <vector>
 
 #include "bgo_internal.cuh"
 
 namespace bgo {
 
-__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
     uint64_t z = x + 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
@@ -34,9 +41,33 @@ struct SynthParams {
     const int64_t *nb_start;  // [n_blocks] sorted, disjoint
     const int64_t *nb_end;
     uint32_t t0, t1, t2;
+    // repeat families (rep_copies == 0: none)
+    int64_t rep_copies, rep_region;
+    int32_t rep_len, rep_families;
+    uint32_t rep_div16;              // substitution probability x 65536
+    uint64_t rep_seed;
+    const uint8_t *rep_seq;          // [rep_families * rep_len] base codes
 };
 
 __device__ __forceinline__ uint32_t gen_base(const SynthParams &p, int64_t pos) {
+    if (p.rep_copies) {
+        const int64_t r = pos / p.rep_region;
+        if (r < p.rep_copies) {
+            const uint64_t h = splitmix64(p.rep_seed * 0xD6E8FEB86659FD93ull + (uint64_t)r);
+            const int64_t start = r * p.rep_region +
+                                  (int64_t)(h % (uint64_t)(p.rep_region - p.rep_len + 1));
+            const int64_t i = pos - start;
+            if (i >= 0 && i < p.rep_len) {
+                const int f = (int)(((h >> 32) & 0xFFFFFFull) % (uint64_t)p.rep_families);
+                const uint8_t *seq = p.rep_seq + (size_t)f * p.rep_len;
+                uint32_t b = (h >> 63) ? 3u - seq[p.rep_len - 1 - i] : seq[i];
+                const uint64_t h2 = splitmix64((p.rep_seed ^ 0xA0761D6478BD642Full) + (uint64_t)pos);
+                if ((uint32_t)(h2 & 0xFFFFu) < p.rep_div16)
+                    b = (b + 1u + (uint32_t)((h2 >> 16) % 3u)) & 3u;
+                return b;
+            }
+        }
+    }
     const uint64_t h = splitmix64(p.seed * 0x9E3779B97F4A7C15ull + (uint64_t)(pos >> 3));
     const uint32_t b = (uint32_t)(h >> (8 * (pos & 7))) & 0xFFu;
     return b < p.t0 ? 0u : b < p.t1 ? 1u : b < p.t2 ? 2u : 3u;
@@ -134,10 +165,10 @@ __global__ void int_probe_kernel(uint32_t *out, uint32_t seed, int iters) {
 
 using namespace bgo;
 
-extern "C" int bgo_synth_genome(uint64_t seed, const int64_t *chrom_lengths, int32_t n_chroms,
-                                const int64_t *n_starts, const int64_t *n_ends, int64_t n_blocks,
-                                const uint8_t *thresholds, int device, uint32_t *fwd_out,
-                                uint32_t *rc_out, uint8_t *n_mask_big_out) {
+static int synth(uint64_t seed, const int64_t *chrom_lengths, int32_t n_chroms,
+                 const int64_t *n_starts, const int64_t *n_ends, int64_t n_blocks,
+                 const uint8_t *thresholds, const bgo_repeat_spec *rep, uint8_t *families_out,
+                 int device, uint32_t *fwd_out, uint32_t *rc_out, uint8_t *n_mask_big_out) {
     if (!chrom_lengths || n_chroms <= 0 || n_blocks < 0 || (n_blocks > 0 && (!n_starts || !n_ends)) ||
         !thresholds || !fwd_out || !rc_out || !n_mask_big_out) {
         set_error("bgo_synth_genome: invalid argument");
@@ -168,6 +199,19 @@ extern "C" int bgo_synth_genome(uint64_t seed, const int64_t *chrom_lengths, int
         set_error("bgo_synth_genome: total length must be < 2^32");
         return BGO_ERR_ARG;
     }
+    std::vector<uint8_t> fam;
+    if (rep && rep->n_copies > 0) {
+        if (rep->n_families <= 0 || rep->family_len <= 0 || rep->divergence_65536 > 65536u ||
+            total / rep->n_copies < rep->family_len || !families_out) {
+            set_error("bgo_synth_genome: repeat families must fit one per region");
+            return BGO_ERR_ARG;
+        }
+        fam.resize((size_t)rep->n_families * rep->family_len);
+        for (size_t i = 0; i < fam.size(); ++i)
+            fam[i] = (uint8_t)(splitmix64(rep->seed * 0x9E3779B97F4A7C15ull + 0x5851F42D4C957F2Dull +
+                                          (uint64_t)i) >> 62);
+        memcpy(families_out, fam.data(), fam.size());
+    }
     BGO_CUDA(cudaSetDevice(device));
     const int64_t n_words = ceil_div(total, 16);
     const int64_t n_bytes = ceil_div(total, 8);
@@ -175,7 +219,8 @@ extern "C" int bgo_synth_genome(uint64_t seed, const int64_t *chrom_lengths, int
     uint8_t *d_mask = nullptr;
     uint32_t *d_fwd = nullptr, *d_rc = nullptr;
     const size_t tab = (size_t)(2 * n_chroms + 2 * n_blocks + 2);
-    cudaError_t e = cudaMalloc(&d_tab, tab * sizeof(int64_t));
+    const size_t tab_bytes = tab * sizeof(int64_t);
+    cudaError_t e = cudaMalloc(&d_tab, tab_bytes + fam.size());
     if (e == cudaSuccess) e = cudaMalloc(&d_mask, (size_t)n_bytes);
     if (e == cudaSuccess) e = cudaMalloc(&d_fwd, (size_t)n_words * 4);
     if (e == cudaSuccess) e = cudaMalloc(&d_rc, (size_t)n_words * 4);
@@ -187,6 +232,18 @@ extern "C" int bgo_synth_genome(uint64_t seed, const int64_t *chrom_lengths, int
     p.t0 = thresholds[0];
     p.t1 = thresholds[1];
     p.t2 = thresholds[2];
+    if (!fam.empty()) {
+        p.rep_copies = rep->n_copies;
+        p.rep_region = total / rep->n_copies;
+        p.rep_len = rep->family_len;
+        p.rep_families = rep->n_families;
+        p.rep_div16 = rep->divergence_65536;
+        p.rep_seed = rep->seed;
+    }
+    if (e == cudaSuccess && !fam.empty()) {
+        p.rep_seq = (const uint8_t *)d_tab + tab_bytes;
+        e = cudaMemcpy((uint8_t *)d_tab + tab_bytes, fam.data(), fam.size(), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) {
         p.offsets = d_tab;
         p.lengths = d_tab + n_chroms;
@@ -222,6 +279,28 @@ extern "C" int bgo_synth_genome(uint64_t seed, const int64_t *chrom_lengths, int
     if (d_rc) cudaFree(d_rc);
     if (e != cudaSuccess) return cuda_fail(e, "bgo_synth_genome");
     return BGO_OK;
+}
+
+extern "C" int bgo_synth_genome(uint64_t seed, const int64_t *chrom_lengths, int32_t n_chroms,
+                                const int64_t *n_starts, const int64_t *n_ends, int64_t n_blocks,
+                                const uint8_t *thresholds, int device, uint32_t *fwd_out,
+                                uint32_t *rc_out, uint8_t *n_mask_big_out) {
+    return synth(seed, chrom_lengths, n_chroms, n_starts, n_ends, n_blocks, thresholds, nullptr,
+                 nullptr, device, fwd_out, rc_out, n_mask_big_out);
+}
+
+extern "C" int bgo_synth_genome_repeats(uint64_t seed, const int64_t *chrom_lengths,
+                                        int32_t n_chroms, const int64_t *n_starts,
+                                        const int64_t *n_ends, int64_t n_blocks,
+                                        const uint8_t *thresholds, const bgo_repeat_spec *repeats,
+                                        uint8_t *families_out, int device, uint32_t *fwd_out,
+                                        uint32_t *rc_out, uint8_t *n_mask_big_out) {
+    if (!repeats) {
+        set_error("bgo_synth_genome_repeats: repeats is NULL");
+        return BGO_ERR_ARG;
+    }
+    return synth(seed, chrom_lengths, n_chroms, n_starts, n_ends, n_blocks, thresholds, repeats,
+                 families_out, device, fwd_out, rc_out, n_mask_big_out);
 }
 
 extern "C" int bgo_probe_int_throughput(int device, int op, double *gops_per_s) {

@@ -85,6 +85,35 @@ def prepare_n_masks(genome: dict) -> Tuple[Optional[np.ndarray], Optional[np.nda
     return fwd, rc
 
 
+def window_cols(g) -> List[int]:
+    """Guide positions of the edit window as Python indexes a 20-nt string:
+    range(start - 1, end) below 20, negative indexes from the end
+    (beguidedoff/base_editing.py:8-27 slices the decoded window this way)."""
+    cols = [i if i >= 0 else 20 + i
+            for i in range(g.edit_window_start - 1, g.edit_window_end) if i < 20]
+    if any(c < 0 for c in cols):
+        raise IndexError("string index out of range")
+    return cols
+
+
+def epilogue_inputs(pairs) -> Optional[np.ndarray]:
+    """Device epilogue rows (bgo_input_row) for (plan row, GuideInput,
+    (on-target chromosome index, local leftmost, strand) or Nones) triples;
+    None if an editor type is unknown (the host path raises its error)."""
+    rows = []
+    for plan_row, g, ot in pairs:
+        tb = TARGET_2BIT.get(g.editor_type)
+        if tb is None:
+            return None
+        mask = 0
+        for c in window_cols(g):
+            mask |= 1 << c
+        has_ot = ot[0] is not None
+        rows.append((plan_row, mask, tb, ot[0] if has_ot else -1, ot[1] if has_ot else 0,
+                     0 if ot[2] == "+" else 1, 0))
+    return np.array(rows, dtype=_native.INPUT_ROW_DTYPE)
+
+
 class beguidedoff:
     """GPU brute-force off-target search (extensive mode)."""
 
@@ -204,16 +233,6 @@ class beguidedoff:
         finally:
             plan.close()
 
-    @staticmethod
-    def _window_cols(g) -> List[int]:
-        """Guide positions of the edit window as Python indexes a 20-nt string:
-        range(start - 1, end) below 20, negative indexes from the end."""
-        cols = [i if i >= 0 else 20 + i
-                for i in range(g.edit_window_start - 1, g.edit_window_end) if i < 20]
-        if any(c < 0 for c in cols):
-            raise IndexError("string index out of range")
-        return cols
-
     def _search_device(self, keys, key_plan, plan_items, mapping, guides, return_all,
                        count_score_threshold, log):
         """Scan + device epilogue; the host only sorts each row's top-N
@@ -230,20 +249,12 @@ class beguidedoff:
             if n > eng.info()["hit_capacity"]:
                 eng.reserve(n)
                 eng.launch(plan, self._strands, ne, self.max_mismatches, self.scan_mode)
-            rows, owners = [], []
-            for ki, key in enumerate(keys):
-                for g in mapping[key]:
-                    tb = TARGET_2BIT.get(g.editor_type)
-                    if tb is None:
-                        return None
-                    mask = 0
-                    for c in self._window_cols(g):
-                        mask |= 1 << c
-                    has_ot = key[2] is not None
-                    rows.append((key_plan[ki], mask, tb, key[2] if has_ot else -1,
-                                 key[3] if has_ot else 0, 0 if key[4] == "+" else 1, 0))
-                    owners.append(g.guide_id)
-            inputs = np.array(rows, dtype=_native.INPUT_ROW_DTYPE)
+            pairs = [(int(key_plan[ki]), g, key[2:]) for ki, key in enumerate(keys)
+                     for g in mapping[key]]
+            inputs = epilogue_inputs(pairs)
+            if inputs is None:
+                return None
+            owners = [g.guide_id for _, g, _ in pairs]
             rank_table, _ = score_ranks()
             below, groups, recs = eng.epilogue(
                 plan, self._strands, inputs, self.chrom_offsets, self.chrom_lengths,
@@ -414,7 +425,7 @@ class beguidedoff:
                 tb = TARGET_2BIT.get(g.editor_type)
                 if tb is None:
                     raise ValueError(f"Unknown editor_type: {g.editor_type}")
-                cols = self._window_cols(g)
+                cols = window_cols(g)
                 if cols and sel.size:
                     editable = (seq[sel][:, cols] == tb).any(axis=1)
                 else:

@@ -151,17 +151,41 @@ def barrier(ws):
 
 MIXED_FAMILIES = (("NGG", 0.40), ("NG", 0.20), ("NNGRRT", 0.15), ("NNNRRT", 0.15),
                   ("NRN", 0.10))
+# hit-dense configuration: repeat families inserted into the genome
+DENSE_REPEATS = {"n_families": 10, "family_len": 300, "n_copies": 200_000, "divergence": 0.10,
+                 "seed": 17}
+DENSE_EDITORS = (("ABE", 4, 8, "ABE8e"), ("CBE", 4, 8, "TadCBEd"), ("CGE", 5, 8, "CGBE"))
+_IUPAC = {"A": "A", "C": "C", "G": "G", "T": "T", "R": "AG", "Y": "CT", "S": "CG", "W": "AT",
+          "K": "GT", "M": "AC", "B": "CGT", "D": "AGT", "H": "ACT", "V": "ACG", "N": "ACGT"}
 
 
 def guide_pams(args, n):
     """PAM of each guide: all NGG (plain configuration) or the mixed-family
-    split of the batched configuration."""
-    if args.config != "mixed":
+    split of the batched and hit-dense configurations."""
+    if args.config == "plain":
         return ["NGG"] * n
     pams = []
     for pam, frac in MIXED_FAMILIES:
         pams += [pam] * int(round(frac * n))
     return (pams + ["NGG"] * n)[:n]
+
+
+def dense_guides(families, pams, seed=3):
+    """Hit-dense guide set: 30% are 20-mers of a repeat consensus followed by a
+    consensus PAM of the guide's family (where the consensus has one), the rest
+    random."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i, pam in enumerate(pams):
+        if i % 10 < 3:
+            fam = families[int(rng.integers(0, len(families)))]
+            ok = [p for p in range(len(fam) - 20 - len(pam))
+                  if all(fam[p + 20 + k] in _IUPAC[c] for k, c in enumerate(pam))]
+            p = ok[int(rng.integers(0, len(ok)))] if ok else int(rng.integers(0, len(fam) - 26))
+            out.append(fam[p:p + 20])
+        else:
+            out.append("".join(rng.choice(list("ACGT"), 20)))
+    return out
 
 
 def plan_arrays(guides, pams=None):
@@ -214,7 +238,10 @@ def bench_reference(args, ws, rank):
     lens, blocks, guides = make_workload(args.genome_bp, args.guides)
     pams = guide_pams(args, len(guides))
     genome = _native.synth_genome(7, lens, blocks, thresholds=(76, 128, 180),
-                                  device=int(os.environ.get("LOCAL_RANK", "0")))
+                                  device=int(os.environ.get("LOCAL_RANK", "0")),
+                                  repeats=DENSE_REPEATS if args.config == "dense" else None)
+    if args.config == "dense":
+        guides = dense_guides(genome["repeat_families"], pams)
     from beguidedoff_gb300.finder import prepare_n_masks
 
     genome["_nm_fwd_le"], genome["_nm_rc_le"] = prepare_n_masks(genome)
@@ -244,6 +271,19 @@ def bench_reference(args, ws, rank):
 
 
 def workload_config(args, lens):
+    if args.config == "dense":
+        name = (f"hit-dense stress: synthetic {int(lens.sum()) / 1e9:.2f} Gbp, 24 chromosomes, "
+                f"GC 41%, 5% N blocks, {DENSE_REPEATS['n_copies']} copies of "
+                f"{DENSE_REPEATS['n_families']} random {DENSE_REPEATS['family_len']}-bp repeat "
+                f"families at {DENSE_REPEATS['divergence']:.0%} divergence, {args.guides} guides "
+                f"(30% from the repeat consensus, mixed PAM families as the batched config), "
+                f"ABE/CBE/CGE windows, max_mismatches {args.max_mm}, both strands; a step = "
+                f"scan + device epilogue (score ranks, window filter, below-threshold counts, "
+                f"top-{3} candidates)")
+        return {"workload": name, "genome_bp": int(lens.sum()), "guides": args.guides,
+                "pam": "mixed", "max_mismatches": args.max_mm, "scan_mode": args.mode,
+                "repeats": DENSE_REPEATS,
+                "l2": "inputs larger than L2 (bit planes of both strands ~2.3 GB)"}
     if args.config == "mixed":
         name = (f"batched mixed-PAM scan: synthetic {int(lens.sum()) / 1e9:.2f} Gbp, "
                 f"24 chromosomes, GC 41%, 5% N blocks, {args.guides} random 20-nt guides "
@@ -279,10 +319,15 @@ def bench_ours(args, ws, rank, local):
     n_words, n_bytes = (total + 15) // 16, (total + 7) // 8
     pin = [_native.HostBuffer((n_words,), np.uint32), _native.HostBuffer((n_words,), np.uint32),
            _native.HostBuffer((n_bytes,), np.uint8)]
+    dense = args.config == "dense"
     t0 = time.perf_counter()
     genome = _native.synth_genome(7, lens, blocks, thresholds=(76, 128, 180), device=local,
-                                  out=[b.array for b in pin])
+                                  out=[b.array for b in pin],
+                                  repeats=DENSE_REPEATS if dense else None)
     t_synth = time.perf_counter() - t0
+    pams = guide_pams(args, len(guides))
+    if dense:
+        guides = dense_guides(genome["repeat_families"], pams)
     t0 = time.perf_counter()
     f = beguidedoff(None, max_mismatches=args.max_mm, genome_data=genome,
                     device=f"cuda:{local}", scan_mode=args.mode)
@@ -292,9 +337,16 @@ def bench_ours(args, ws, rank, local):
         hb = _native.HostBuffer((m.size,), np.uint8)
         hb.array[:] = m
         nm_pin.append(hb)
-    pams = guide_pams(args, len(guides))
     gv, pm, pl, p3 = plan_arrays(guides, pams)
     plan = _native.Plan(f._engine, gv, pm, pl, p3)
+    plan.set_tuning(args.chunk_sites, args.group_guides, args.ctas_per_sm)
+    if dense:
+        editors = [DENSE_EDITORS[i % 3] for i in range(len(guides))]
+    else:
+        editors = [("ABE", 4, 8, "ABE8e") if i % 2 == 0 else ("CBE", 4, 8, "TadCBEd")
+                   for i in range(len(guides))]
+    ginputs = [GuideInput(f"row_{i}", g, pams[i], "3prime", e[1], e[2], e[0], base_editor=e[3])
+               for i, (g, e) in enumerate(zip(guides, editors))]
     eng = f._engine
     comps = args.guides * 2 * (total - 26)
 
@@ -321,11 +373,31 @@ def bench_ours(args, ws, rank, local):
 
     # -------- device-resident kernel timing (value) --------
     graph = None
-    if args.mode == 2 and not args.no_graph:
-        graph = _native.Graph(eng, plan, f._strands, [0, 3], args.max_mm, 2)
-        step = lambda: graph.replay(sp)  # noqa: E731
+    if args.mode in (2, 3) and not args.no_graph:
+        graph = _native.Graph(eng, plan, f._strands, [0, 3], args.max_mm, args.mode)
+        scan_step = lambda: graph.replay(sp)  # noqa: E731
     else:
-        step = lambda: eng.launch(plan, f._strands, [0, 3], args.max_mm, args.mode, sp)  # noqa: E731
+        scan_step = lambda: eng.launch(plan, f._strands, [0, 3], args.max_mm, args.mode, sp)  # noqa: E731
+    step = scan_step
+    epi = None
+    if dense:
+        from beguidedoff_gb300.finder import epilogue_inputs
+        from beguidedoff_gb300.scoring import score_ranks, threshold_rank
+
+        inputs = epilogue_inputs([(i, g, (None, None, None)) for i, g in enumerate(ginputs)])
+        rank_table, _ = score_ranks()
+        thr_rank = threshold_rank(5.0)
+        scan_step()
+        n_raw = eng.hit_count(sp)
+        if n_raw > eng.info()["hit_capacity"]:
+            eng.reserve(n_raw)
+        epi = {"records": 0}
+
+        def step():
+            scan_step()
+            _, _, recs = eng.epilogue(plan, f._strands, inputs, f.chrom_offsets,
+                                      f.chrom_lengths, rank_table, thr_rank, 3, False, sp)
+            epi["records"] = int(recs.size)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -337,6 +409,12 @@ def bench_ours(args, ws, rank, local):
     barrier(ws)
     clk = clocks.stop()
     launches = eng.launch_count() - n0
+    if dense:
+        # the scan alone, to split the step between scan and epilogue
+        scan_ms, scan_total = timed(scan_step, args.steps)
+        epi.update({"scan_ms_per_step": scan_total / args.steps,
+                    "epilogue_ms_per_step": (total_ms - scan_total) / args.steps,
+                    "raw_hits_per_step": eng.hit_count(sp)})
     t_max = dist_max(total_ms / 1e3, ws)
     hits = eng.hit_count(sp)
     pairs = eng.pairs_evaluated(sp)
@@ -361,9 +439,6 @@ def bench_ours(args, ws, rank, local):
     hbm_achieved = plane_bytes / (total_ms / 1e3 / args.steps) / 1e9
 
     # -------- end to end through the public API, genome uploaded each step --------
-    ginputs = [GuideInput(f"row_{i}", g, pams[i], "3prime", 4, 8, "ABE" if i % 2 == 0 else "CBE",
-                          base_editor="ABE8e" if i % 2 == 0 else "TadCBEd")
-               for i, g in enumerate(guides)]
     for s in f._strands:
         s.close()
 
@@ -379,15 +454,18 @@ def bench_ours(args, ws, rank, local):
     torch.cuda.synchronize()
     barrier(ws)
     n1 = eng.launch_count()
+    x0 = eng.transfer()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         table = e2e_step()
     torch.cuda.synchronize()
     e2e_s = dist_max((time.perf_counter() - t0) / args.steps, ws)
     e2e_launches = eng.launch_count() - n1
+    x1 = eng.transfer()
+    # strand uploads (counted from the arrays) + what the engine's calls copied
     h2d = (pin[0].array.nbytes + pin[1].array.nbytes + nm_pin[0].array.nbytes
-           + nm_pin[1].array.nbytes + gv.nbytes + pm.nbytes + pl.nbytes + p3.nbytes)
-    d2h = 8 * hits + 8
+           + nm_pin[1].array.nbytes + (x1["h2d"] - x0["h2d"]) // args.steps)
+    d2h = (x1["d2h"] - x0["d2h"]) // args.steps
 
     # -------- CPU baseline (oracle, all host cores, bounded sample) --------
     cpu = None
@@ -403,7 +481,7 @@ def bench_ours(args, ws, rank, local):
         popc = {"achieved_gops": achieved, "peak_gops": popc_peak, "frac": achieved / popc_peak,
                 "compares_per_step": pairs, "lop3_peak_gops": lop3_peak,
                 "peak_source": "measured live: bgo_probe_int_throughput"}
-        if args.mode == 2:
+        if args.mode in (2, 3):
             # the segment index makes the compares sub-linear in guides: the
             # floor of a full scan is streaming both strands' planes once
             roof = {"bound": "hbm", "unit": "GB/s", "achieved": hbm_achieved, "peak": hbm_peak,
@@ -430,6 +508,8 @@ def bench_ours(args, ws, rank, local):
                     "d2h_bytes_per_step": d2h, "s_per_step": e2e_s,
                     "rows": len(table), "launches": e2e_launches // args.steps},
             "gpu_launches": launches,
+            "tuning": getattr(plan, "tuning", None),
+            "epilogue": epi,
             "graph": graph is not None,
             "plain_form": plain,
             "speedup_vs_plain": (plain["ms_per_step"] / (1e3 * t_max / args.steps)
@@ -452,23 +532,27 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", type=int, default=2, choices=[0, 1, 2])
+    ap.add_argument("--mode", type=int, default=2, choices=[0, 1, 2, 3])
+    ap.add_argument("--chunk-sites", type=int, default=0, help="modes 2/3 tile length (0 = default)")
+    ap.add_argument("--group-guides", type=int, default=0, help="mode 3 guides per group")
+    ap.add_argument("--ctas-per-sm", type=int, default=0)
     ap.add_argument("--genome-bp", type=int, default=3_100_000_000)
     ap.add_argument("--guides", type=int, default=100)
     ap.add_argument("--max-mm", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
-    ap.add_argument("--config", default="plain", choices=["plain", "mixed"],
-                    help="plain: 100 NGG guides, <=4 mm; mixed: 400 mixed-PAM guides, <=5 mm")
+    ap.add_argument("--config", default="plain", choices=["plain", "mixed", "dense"],
+                    help="plain: 100 NGG guides, <=4 mm; mixed: 400 mixed-PAM guides, <=5 mm; "
+                         "dense: repeat-family genome, 1000 mixed guides, <=6 mm")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.config == "mixed":
+    if args.config in ("mixed", "dense"):
         if "--guides" not in sys.argv:
-            args.guides = 400
+            args.guides = 400 if args.config == "mixed" else 1000
         if "--max-mm" not in sys.argv:
-            args.max_mm = 5
+            args.max_mm = 5 if args.config == "mixed" else 6
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         bench_reference(args, ws, rank)

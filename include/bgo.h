@@ -106,7 +106,14 @@ int bgo_plan_info(const bgo_plan *plan, int32_t *n_families, int32_t *n_guides);
  * an N encodes as on strand s (0 forward, 3 reverse complement).  Positions
  * scanned: [0, total_bp - 26) of each strand, as the reference kernel.
  * mode: 0 = one kernel per PAM family and strand (plain form),
- *       1 = one persistent launch over all families and strands.
+ *       1 = one persistent launch over all families and strands, every guide
+ *           compared at every PAM-passing position,
+ *       2 = one launch with a segment index (pigeonhole over max_mismatches + 1
+ *           segments, bucket lists of guides) for max_mismatches <= 7,
+ *       3 = one launch with the segment index stored as guide bitmasks.
+ * All modes return the same hits.  Modes 2 and 3 run as mode 1 when their
+ * index does not apply (max_mismatches > 7 or an index too large for shared
+ * memory).
  */
 int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genome *const *strands,
                     const int32_t *n_encoded, int32_t n_strands, int32_t max_mismatches,
@@ -127,12 +134,32 @@ int bgo_scan_collect(bgo_engine *engine, uint64_t *keys, int64_t capacity, int64
 int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
 
 /*
+ * Launch parameters of a plan (scan modes 2 and 3), normally chosen by the
+ * autotuner (beguidedoff_gb300/autotune.py).  Zero fields keep the defaults.
+ *   chunk_sites   positions per warp chunk ("tile length"): 1024 or 2048
+ *   group_guides  mode 3: guides per mask group ("guides per block"): 32, 64
+ *                 or 128; a family larger than this is cut into several groups
+ *   ctas_per_sm   cap on resident CTAs per SM for the grid size (0 = the
+ *                 occupancy maximum)
+ * Changing group_guides rebuilds the mask index at the next launch.  No
+ * reference counterpart: the reference fixes 256 threads x 200 Mbp chunks.
+ */
+typedef struct bgo_tuning {
+    int32_t chunk_sites;
+    int32_t group_guides;
+    int32_t ctas_per_sm;
+    int32_t reserved;
+} bgo_tuning;
+int bgo_plan_set_tuning(bgo_plan *plan, const bgo_tuning *tuning);
+
+/*
  * The same scan as bgo_scan_launch, captured once into a CUDA graph and
  * replayed by bgo_graph_launch (each replay resets the engine's counters and
  * rescans; collect with bgo_scan_collect).  Everything that allocates or
  * synchronises (the segment index, kernel attributes) happens at creation.
  * The graph refers to the engine, plan and strands: keep them alive and
- * unchanged while it exists; bgo_engine_reserve invalidates it.  No
+ * unchanged while it exists.  After bgo_engine_reserve moved the hit buffer,
+ * the next bgo_graph_launch captures the scan again before it runs.  No
  * reference counterpart: the reference launches one kernel per 200 Mbp chunk.
  */
 typedef struct bgo_graph bgo_graph;
@@ -204,6 +231,12 @@ int bgo_search_genome(bgo_engine *engine, const bgo_genome *strand, const uint64
  * creation (diagnostics); either pointer may be NULL. */
 int bgo_engine_info(const bgo_engine *engine, int64_t *hit_capacity, int64_t *n_launches);
 
+/* Bytes the engine's calls have copied host -> device (plans, segment
+ * indexes, epilogue inputs and the score-rank table when it changes) and
+ * device -> host (hit counts, keys, epilogue results) since creation.  Strand
+ * uploads (bgo_genome_create) are not engine calls and are not counted. */
+int bgo_engine_transfer(const bgo_engine *engine, int64_t *h2d_bytes, int64_t *d2h_bytes);
+
 /*
  * The scan for callers that cannot allocate device memory: programs whose own
  * allocator already owns the GPU's memory, and latency-critical loops where a
@@ -243,6 +276,31 @@ int bgo_synth_genome(uint64_t seed, const int64_t *chrom_lengths, int32_t n_chro
                      const int64_t *n_starts, const int64_t *n_ends, int64_t n_blocks,
                      const uint8_t *thresholds, int device, uint32_t *fwd_out, uint32_t *rc_out,
                      uint8_t *n_mask_big_out);
+
+/*
+ * Repeat families inserted by bgo_synth_genome_repeats: the genome is cut
+ * into n_copies equal regions; region r holds one copy of a seeded family at a
+ * seeded offset and orientation, each base substituted with probability
+ * divergence_65536 / 65536.  Families are uniform random ACGT of family_len bp.
+ */
+typedef struct bgo_repeat_spec {
+    int32_t n_families;
+    int32_t family_len;
+    int64_t n_copies;
+    uint32_t divergence_65536;
+    uint32_t reserved;
+    uint64_t seed;
+} bgo_repeat_spec;
+
+/*
+ * bgo_synth_genome with repeat families (the hit-dense workload).
+ * families_out receives n_families * family_len base codes (0-3 = ACGT).
+ */
+int bgo_synth_genome_repeats(uint64_t seed, const int64_t *chrom_lengths, int32_t n_chroms,
+                             const int64_t *n_starts, const int64_t *n_ends, int64_t n_blocks,
+                             const uint8_t *thresholds, const bgo_repeat_spec *repeats,
+                             uint8_t *families_out, int device, uint32_t *fwd_out,
+                             uint32_t *rc_out, uint8_t *n_mask_big_out);
 
 /*
  * Measured throughput (Gop/s) of one integer instruction on `device`:

@@ -25,7 +25,7 @@ def _lib():
 
 
 @pytest.mark.parametrize("mode,epilogue", [(0, "device"), (1, "device"), (2, "device"),
-                                           (2, "host")])
+                                           (3, "device"), (2, "host")])
 @pytest.mark.parametrize("name", FINDER_CASES)
 def test_finder_tables_match_reference(name, mode, epilogue):
     case = Case(name)
@@ -146,10 +146,36 @@ def test_random_mixed_pam_keys_equal_oracle(seed):
     assert exp.size > 100
     f = beguidedoff(None, max_mismatches=5, genome_data=genome)
     try:
-        for mode in (0, 1, 2):
+        for mode in (0, 1, 2, 3):
             f.scan_mode = mode
             got = f._scan(seqs, pams)
             assert got.size == exp.size and np.array_equal(got, exp), mode
+    finally:
+        f.close()
+
+
+@pytest.mark.parametrize("k", [0, 1, 2, 3, 6, 7])
+def test_indexed_modes_every_k_equal_oracle(k):
+    """Segment index (mode 2) and segment masks (mode 3) at every segment
+    layout they compile, against the oracle; mode 3 also at each tuning."""
+    genome, rng = _random_genome(40 + k, [400_000, 260_001])
+    seqs, pams = [], []
+    for i in range(70):
+        s = "".join(rng.choice(list("ACGT"), 20))
+        pam = MIXED_PAMS[i % len(MIXED_PAMS)]
+        _plant(genome, rng, s, pam, 3, min(k, 5))
+        seqs.append(s)
+        pams.append(pam)
+    exp = oracle_keys(genome, seqs, pams, k)
+    f = beguidedoff(None, max_mismatches=k, genome_data=genome)
+    try:
+        plan = f._plan(seqs, pams)
+        tunings = [(0, 0, 0), (1024, 32, 0), (2048, 64, 2), (1024, 128, 1)]
+        for mode, tune in [(2, (0, 0, 0))] + [(3, t) for t in tunings]:
+            plan.set_tuning(*tune)
+            got = f._engine.scan(plan, f._strands, [0, 3], k, mode)
+            assert got.size == exp.size and np.array_equal(got, exp), (mode, tune)
+        plan.close()
     finally:
         f.close()
 
@@ -225,13 +251,42 @@ def test_graph_replay_equals_launch():
                 pm[i, j] = IUPAC[ch]
         pl = np.array([len(p) for p in pams], dtype=np.uint8)
         plan = _native.Plan(f._engine, gv, pm, pl, np.ones(len(seqs), dtype=np.uint8))
-        for mode in (0, 2):
+        for mode in (0, 2, 3):
             g = _native.Graph(f._engine, plan, f._strands, [0, 3], 5, mode)
             for _ in range(2):
                 g.replay()
                 n, keys = f._engine.collect()
                 assert n == exp.size and np.array_equal(keys, exp), mode
             g.close()
+        plan.close()
+    finally:
+        f.close()
+
+
+def test_graph_recaptures_after_hit_buffer_grows():
+    """A graph captured before bgo_engine_reserve moved the hit buffer must
+    not write to the old buffer: the next replay captures again and returns
+    the exact keys."""
+    unit = "T" + "ACGTACGTACGTACGTACGT"[1:] + "AGG"
+    from beguidedoff_gb300.genome_converter import encode_chromosomes
+
+    g = encode_chromosomes([("chr1", (unit * 1_100_000 + "A" * 30).encode())])
+    exp = oracle_keys(g, ["ACGTACGTACGTACGTACGT"], ["NGG"], 4)
+    f = beguidedoff(None, max_mismatches=4, genome_data=g)
+    try:
+        cap0 = f._engine.info()["hit_capacity"]
+        assert exp.size > cap0
+        plan = f._plan(["ACGTACGTACGTACGTACGT"], ["NGG"])
+        for mode in (3, 2, 1):
+            gr = _native.Graph(f._engine, plan, f._strands, [0, 3], 4, mode)
+            gr.replay()
+            n, keys = f._engine.collect()
+            if keys is None:
+                f._engine.reserve(n)
+            gr.replay()
+            n, keys = f._engine.collect()
+            assert keys is not None and np.array_equal(keys, exp), mode
+            gr.close()
         plan.close()
     finally:
         f.close()
