@@ -27,13 +27,16 @@ EXPORTED = [
     "bgo_engine_info", "bgo_synth_genome", "bgo_probe_int_throughput", "bgo_scan_stats",
     "bgo_scan_noalloc", "bgo_graph_create", "bgo_graph_launch", "bgo_graph_destroy",
     "bgo_epilogue_run", "bgo_synth_genome_repeats", "bgo_engine_transfer",
-    "bgo_plan_set_tuning",
+    "bgo_plan_set_tuning", "bgo_epilogue_fetch",
 ]
 
 INPUT_ROW_DTYPE = np.dtype([("plan_row", "<i4"), ("window_mask", "<u4"), ("target_base", "<i4"),
                             ("ot_chrom", "<i4"), ("ot_local", "<i8"), ("ot_strand", "<i4"),
-                            ("pad", "<i4")])
-RECORD_DTYPE = np.dtype([("key", "<u8"), ("input_row", "<i4"), ("rank", "<u4")])
+                            ("threshold_rank", "<i4"), ("flags", "<i4"), ("pad", "<i4")])
+ROW_RETURN_ALL = 1
+RECORD_DTYPE = np.dtype([("key", "<u8"), ("order", "<u8"), ("input_row", "<i4"),
+                         ("rank", "<u4")])
+assert INPUT_ROW_DTYPE.itemsize == 40 and RECORD_DTYPE.itemsize == 24
 
 NOALLOC_MAX_GUIDES = 2048
 NOALLOC_MAX_HITS = 1 << 20
@@ -77,8 +80,9 @@ _SIGS = {
     "bgo_graph_create": ([_P, _P, _P, _P, _I32, _I32, _I32, _PP], ctypes.c_int),
     "bgo_graph_launch": ([_P, _P], ctypes.c_int),
     "bgo_graph_destroy": ([_P], ctypes.c_int),
-    "bgo_epilogue_run": ([_P, _P, _P, _I32, _P, _I32, _P, _P, _I32, _P, _I32, _I32, _I32, _P, _P,
-                          _P, _I64, ctypes.POINTER(_I64), _P], ctypes.c_int),
+    "bgo_epilogue_run": ([_P, _P, _P, _I32, _P, _I32, _P, _P, _P, _I32, _P, _I32, _P, _P, _P,
+                          ctypes.POINTER(_I64), _P], ctypes.c_int),
+    "bgo_epilogue_fetch": ([_P, _P, _I64, _P], ctypes.c_int),
     "bgo_scan_noalloc": ([_P, _P, _I32, _P, _P, _P, _P, _I32, _I32, _P, _I64,
                           ctypes.POINTER(_I64), _P], ctypes.c_int),
     "bgo_engine_reserve": ([_P, _I64], ctypes.c_int),
@@ -390,30 +394,30 @@ class Engine:
               "bgo_engine_transfer")
         return {"h2d": a.value, "d2h": b.value}
 
-    def epilogue(self, plan, strands, inputs, chrom_offsets, chrom_lengths, rank_table,
-                 threshold_rank, n_top, return_all, stream=None):
-        """Device epilogue of the last scan: (below[n_inputs], group_counts
-        [n_plan_rows, 2], records) - see bgo_epilogue_run."""
+    def epilogue(self, plan, strands, inputs, chrom_offsets, chrom_lengths, chrom_rank,
+                 rank_table, n_top, stream=None):
+        """Device epilogue of the last scan (bgo_epilogue_run + fetch):
+        (below[n_inputs], group_counts[n_plan_rows, 2], row_counts[n_inputs],
+        records grouped by input row)."""
         inputs = np.ascontiguousarray(inputs, dtype=INPUT_ROW_DTYPE)
         offs = np.ascontiguousarray(chrom_offsets, dtype=np.int64)
         lens = np.ascontiguousarray(chrom_lengths, dtype=np.int64)
+        crank = np.ascontiguousarray(chrom_rank, dtype=np.int32)
         rt = np.ascontiguousarray(rank_table, dtype=np.uint32)
         arr = (ctypes.c_void_p * len(strands))(*[s.handle.value for s in strands])
         below = np.zeros(max(inputs.size, 1), dtype=np.int64)
+        counts = np.zeros(max(inputs.size, 1), dtype=np.int64)
         groups = np.zeros(max(2 * plan.n_guides, 2), dtype=np.int64)
-        cap = 1 << 16
-        while True:
-            recs = np.zeros(cap, dtype=RECORD_DTYPE)
-            n = ctypes.c_int64()
-            check(lib().bgo_epilogue_run(
-                self.handle, plan.handle, arr, len(strands), ptr(inputs), inputs.size,
-                ptr(offs), ptr(lens), offs.size, ptr(rt), int(threshold_rank), int(n_top),
-                int(bool(return_all)), below.ctypes.data, groups.ctypes.data, recs.ctypes.data,
-                cap, ctypes.byref(n), stream), "bgo_epilogue_run")
-            if n.value <= cap:
-                return (below[:inputs.size], groups[:2 * plan.n_guides].reshape(-1, 2),
-                        recs[:n.value])
-            cap = int(n.value) + 1024
+        n = ctypes.c_int64()
+        check(lib().bgo_epilogue_run(
+            self.handle, plan.handle, arr, len(strands), ptr(inputs), inputs.size, ptr(offs),
+            ptr(lens), ptr(crank), offs.size, ptr(rt), int(n_top), below.ctypes.data,
+            groups.ctypes.data, counts.ctypes.data, ctypes.byref(n), stream), "bgo_epilogue_run")
+        recs = np.zeros(n.value, dtype=RECORD_DTYPE)
+        check(lib().bgo_epilogue_fetch(self.handle, recs.ctypes.data if n.value else None,
+                                       n.value, stream), "bgo_epilogue_fetch")
+        return (below[:inputs.size], groups[:2 * plan.n_guides].reshape(-1, 2),
+                counts[:inputs.size], recs)
 
     def close(self):
         if self.handle is not None and self.handle.value:

@@ -243,6 +243,11 @@ struct bgo_engine {
     // epilogue: grow-only scratch and the device copy of the score-rank table
     unsigned char *d_epi = nullptr;
     size_t epi_bytes = 0;
+    unsigned char *d_epi_rec = nullptr;   // candidate records, grouped by input row
+    size_t epi_rec_bytes = 0;
+    unsigned char *d_epi_out = nullptr;   // kept records, dense, for bgo_epilogue_fetch
+    size_t epi_out_bytes = 0;
+    int64_t epi_out_n = -1;               // records of the last epilogue (-1: none)
     uint32_t *d_rank = nullptr;
     std::vector<uint32_t> h_rank;   // host copy of what d_rank holds
     // bytes copied host -> device and device -> host by engine calls

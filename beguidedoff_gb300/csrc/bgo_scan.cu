@@ -245,6 +245,8 @@ extern "C" int bgo_engine_destroy(bgo_engine *e) {
     if (e->d_keys) cudaFree(e->d_keys);
     if (e->d_counter) cudaFree(e->d_counter);
     if (e->d_epi) cudaFree(e->d_epi);
+    if (e->d_epi_rec) cudaFree(e->d_epi_rec);
+    if (e->d_epi_out) cudaFree(e->d_epi_out);
     if (e->d_rank) cudaFree(e->d_rank);
     delete e;
     return BGO_OK;

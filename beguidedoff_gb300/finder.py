@@ -96,11 +96,13 @@ def window_cols(g) -> List[int]:
     return cols
 
 
-def epilogue_inputs(pairs) -> Optional[np.ndarray]:
+def epilogue_inputs(pairs, threshold_rank: int = -1, return_all: bool = False
+                    ) -> Optional[np.ndarray]:
     """Device epilogue rows (bgo_input_row) for (plan row, GuideInput,
     (on-target chromosome index, local leftmost, strand) or Nones) triples;
     None if an editor type is unknown (the host path raises its error)."""
     rows = []
+    flags = _native.ROW_RETURN_ALL if return_all else 0
     for plan_row, g, ot in pairs:
         tb = TARGET_2BIT.get(g.editor_type)
         if tb is None:
@@ -110,7 +112,7 @@ def epilogue_inputs(pairs) -> Optional[np.ndarray]:
             mask |= 1 << c
         has_ot = ot[0] is not None
         rows.append((plan_row, mask, tb, ot[0] if has_ot else -1, ot[1] if has_ot else 0,
-                     0 if ot[2] == "+" else 1, 0))
+                     0 if ot[2] == "+" else 1, threshold_rank, flags, 0))
     return np.array(rows, dtype=_native.INPUT_ROW_DTYPE)
 
 
@@ -251,15 +253,14 @@ class beguidedoff:
                 eng.launch(plan, self._strands, ne, self.max_mismatches, self.scan_mode)
             pairs = [(int(key_plan[ki]), g, key[2:]) for ki, key in enumerate(keys)
                      for g in mapping[key]]
-            inputs = epilogue_inputs(pairs)
+            inputs = epilogue_inputs(pairs, threshold_rank(count_score_threshold), return_all)
             if inputs is None:
                 return None
             owners = [g.guide_id for _, g, _ in pairs]
             rank_table, _ = score_ranks()
-            below, groups, recs = eng.epilogue(
+            below, groups, _, recs = eng.epilogue(
                 plan, self._strands, inputs, self.chrom_offsets, self.chrom_lengths,
-                rank_table, threshold_rank(count_score_threshold), self.n_top_offtargets,
-                return_all)
+                self._chrom_rank, rank_table, self.n_top_offtargets)
         finally:
             plan.close()
         counts_k = groups[key_plan]

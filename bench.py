@@ -384,9 +384,9 @@ def bench_ours(args, ws, rank, local):
         from beguidedoff_gb300.finder import epilogue_inputs
         from beguidedoff_gb300.scoring import score_ranks, threshold_rank
 
-        inputs = epilogue_inputs([(i, g, (None, None, None)) for i, g in enumerate(ginputs)])
+        inputs = epilogue_inputs([(i, g, (None, None, None)) for i, g in enumerate(ginputs)],
+                                 threshold_rank(5.0), False)
         rank_table, _ = score_ranks()
-        thr_rank = threshold_rank(5.0)
         scan_step()
         n_raw = eng.hit_count(sp)
         if n_raw > eng.info()["hit_capacity"]:
@@ -395,8 +395,8 @@ def bench_ours(args, ws, rank, local):
 
         def step():
             scan_step()
-            _, _, recs = eng.epilogue(plan, f._strands, inputs, f.chrom_offsets,
-                                      f.chrom_lengths, rank_table, thr_rank, 3, False, sp)
+            _, _, _, recs = eng.epilogue(plan, f._strands, inputs, f.chrom_offsets,
+                                         f.chrom_lengths, f._chrom_rank, rank_table, 3, sp)
             epi["records"] = int(recs.size)
     for _ in range(args.warmup):
         step()

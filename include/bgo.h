@@ -176,40 +176,54 @@ int bgo_graph_destroy(bgo_graph *graph);
  * (the reference's GuideInput after dedup to a plan row).
  *   rank_table[mask]  rank of the exact CCTOP score of each 20-bit mismatch
  *                     mask (bit p-1 = position p) among all distinct scores,
- *                     ascending; 2^20 entries, built on the host;
- *   threshold_rank    hits with rank <= it count as below the score threshold
- *                     (-1: no threshold);
- *   n_top, return_all the reference's top-N rule.
- * Outputs: below[n_inputs] = the reference's n_offtargets_below_threshold;
- * group_counts[2 * n_plan_rows] = hits per (plan row, strand slot); records =
- * for every input row every included hit (editable, or any with return_all;
- * on-target excluded) whose score rank is in the histogram bins up to the one
- * holding its n_top-th hit - a superset of its top n_top that the caller
- * sorts exactly.  *n_records is exact; nothing is copied if it exceeds
- * capacity.
+ *                     ascending; 2^20 entries, built on the host (uploaded
+ *                     once per engine while it does not change);
+ *   chrom_rank[c]     rank of chromosome c's name in sorted name order (the
+ *                     reference's tie order after the score);
+ *   n_top             the reference's top-N rule.
+ * A hit's order key is (score rank, chromosome name rank, local report
+ * position, strand) packed in 64 bits - the reference's sort order.  Per input
+ * row the epilogue keeps every included hit (editable, or any hit when the
+ * row's flags ask for all; on-target excluded) among the row's n_top smallest
+ * order keys, all of them when the row returns all.  With more than 1024
+ * chromosomes the key holds the score rank only and all hits tied at the n_top
+ * boundary are kept (the caller sorts them).
+ * Outputs (host): below[n_inputs] = the reference's n_offtargets_below_threshold;
+ * group_counts[2 * n_plan_rows] = hits per (plan row, strand slot);
+ * row_counts[n_inputs] = records kept per input row; *n_records = their sum.
+ * The records stay on the device, grouped by input row in row order, until
+ * bgo_epilogue_fetch copies them.
  */
 typedef struct {
-    int32_t plan_row;     /* plan row of this input row's scan key             */
-    uint32_t window_mask; /* bit p-1: window position p is in the edit window  */
-    int32_t target_base;  /* 0 = A (ABE), 1 = C (CBE, CGE)                      */
-    int32_t ot_chrom;     /* on-target chromosome index, -1 = no exclusion      */
-    int64_t ot_local;     /* on-target local leftmost position (0-based)        */
-    int32_t ot_strand;    /* on-target strand slot: 0 '+', 1 '-'                */
+    int32_t plan_row;       /* plan row of this input row's scan key             */
+    uint32_t window_mask;   /* bit p-1: window position p is in the edit window  */
+    int32_t target_base;    /* 0 = A (ABE), 1 = C (CBE, CGE)                      */
+    int32_t ot_chrom;       /* on-target chromosome index, -1 = no exclusion      */
+    int64_t ot_local;       /* on-target local leftmost position (0-based)        */
+    int32_t ot_strand;      /* on-target strand slot: 0 '+', 1 '-'                */
+    int32_t threshold_rank; /* hits with rank <= it count as below the threshold
+                               (-1: no threshold)                                 */
+    int32_t flags;          /* BGO_ROW_RETURN_ALL: keep every included hit        */
     int32_t pad;
 } bgo_input_row;
+#define BGO_ROW_RETURN_ALL 1
 
 typedef struct {
     uint64_t key;      /* the hit key */
-    int32_t input_row; /* input row the hit is a candidate for */
+    uint64_t order;    /* the hit's order key for its input row */
+    int32_t input_row; /* input row the hit is kept for */
     uint32_t rank;     /* rank of its CCTOP score */
 } bgo_record;
 
 int bgo_epilogue_run(bgo_engine *engine, const bgo_plan *plan, const bgo_genome *const *strands,
                      int32_t n_strands, const bgo_input_row *inputs, int32_t n_inputs,
-                     const int64_t *chrom_offsets, const int64_t *chrom_lengths, int32_t n_chroms,
-                     const uint32_t *rank_table, int32_t threshold_rank, int32_t n_top,
-                     int32_t return_all, int64_t *below, int64_t *group_counts,
-                     bgo_record *records, int64_t capacity, int64_t *n_records, void *stream);
+                     const int64_t *chrom_offsets, const int64_t *chrom_lengths,
+                     const int32_t *chrom_rank, int32_t n_chroms, const uint32_t *rank_table,
+                     int32_t n_top, int64_t *below, int64_t *group_counts, int64_t *row_counts,
+                     int64_t *n_records, void *stream);
+
+/* Copies the records of the last bgo_epilogue_run (capacity >= its n_records). */
+int bgo_epilogue_fetch(bgo_engine *engine, bgo_record *records, int64_t capacity, void *stream);
 
 /* Grows the engine's device hit buffer to at least `n_hits` keys. */
 int bgo_engine_reserve(bgo_engine *engine, int64_t n_hits);

@@ -231,6 +231,43 @@ def test_device_epilogue_tables_equal_host_assembly(seed):
         f.close()
 
 
+def test_device_epilogue_ties_and_chromosome_order():
+    """Tens of thousands of hits tied on score across chromosomes whose names
+    sort differently from their order: the device's order keys (score rank,
+    name rank, local position, strand) and radix select give the host
+    assembly's exact top-N."""
+    from beguidedoff_gb300.genome_converter import encode_chromosomes
+
+    unit = "T" + "ACGTACGTACGTACGTACGT"[1:] + "AGG"
+    rng = np.random.default_rng(3)
+    chroms = []
+    for name, reps in (("chr10", 9000), ("chr2", 7000), ("chrX", 5000), ("chr1", 8000)):
+        body = list(unit * reps)
+        for p in rng.choice(len(body), size=len(body) // 40, replace=False):
+            body[p] = "ACGT"[int(rng.integers(0, 4))]
+        chroms.append((name, "".join(body).encode()))
+    g = encode_chromosomes(chroms)
+    guide = "ACGTACGTACGTACGTACGT"
+    host = beguidedoff.host_only(g, 4)
+    host._scan = lambda sq, pm: oracle_keys(g, sq, pm, 4)
+    guides = [GuideInput("a", guide, "NGG", "3prime", 4, 8, "ABE"),
+              GuideInput("b", guide, "NGG", "3prime", 1, 20, "CBE", on_target_chrom="chr2",
+                         on_target_pos=24, on_target_strand="+"),
+              GuideInput("a", guide, "NGN", "3prime", 2, 6, "CGE")]
+    f = beguidedoff(None, max_mismatches=4, genome_data=g, results_per_guide=10_000_000)
+    host.results_per_guide = 10_000_000
+    try:
+        for n_top in (1, 3, 7, 200):
+            f.n_top_offtargets = host.n_top_offtargets = n_top
+            for kw in ({}, {"count_score_threshold": 3.0}, {"return_all": True}):
+                exp = table_rows(host.search(guides=guides, verbose=False, **kw))
+                got = table_rows(f.search(guides=guides, verbose=False, **kw))
+                ok, why = rows_equal(got, exp)
+                assert ok, f"n_top {n_top} {kw}: {why}"
+    finally:
+        f.close()
+
+
 def test_graph_replay_equals_launch():
     """A captured scan (bgo_graph_create / bgo_graph_launch) returns the same
     keys as ordinary launches, on every replay, for the plain and indexed forms."""
