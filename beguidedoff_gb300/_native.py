@@ -27,7 +27,7 @@ EXPORTED = [
     "bgo_engine_info", "bgo_synth_genome", "bgo_probe_int_throughput", "bgo_scan_stats",
     "bgo_scan_noalloc", "bgo_graph_create", "bgo_graph_launch", "bgo_graph_destroy",
     "bgo_epilogue_run", "bgo_synth_genome_repeats", "bgo_engine_transfer",
-    "bgo_plan_set_tuning", "bgo_epilogue_fetch",
+    "bgo_plan_set_tuning", "bgo_epilogue_fetch", "bgo_scan_time",
 ]
 
 INPUT_ROW_DTYPE = np.dtype([("plan_row", "<i4"), ("window_mask", "<u4"), ("target_base", "<i4"),
@@ -83,6 +83,8 @@ _SIGS = {
     "bgo_epilogue_run": ([_P, _P, _P, _I32, _P, _I32, _P, _P, _P, _I32, _P, _I32, _P, _P, _P,
                           ctypes.POINTER(_I64), _P], ctypes.c_int),
     "bgo_epilogue_fetch": ([_P, _P, _I64, _P], ctypes.c_int),
+    "bgo_scan_time": ([_P, _P, _P, _P, _I32, _I32, _I32, _I32, _P,
+                       ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "bgo_scan_noalloc": ([_P, _P, _I32, _P, _P, _P, _P, _I32, _I32, _P, _I64,
                           ctypes.POINTER(_I64), _P], ctypes.c_int),
     "bgo_engine_reserve": ([_P, _I64], ctypes.c_int),
@@ -273,7 +275,7 @@ class Strand:
 class Tuning(ctypes.Structure):
     """bgo_tuning: launch parameters of scan modes 2 and 3 (0 = default)."""
     _fields_ = [("chunk_sites", ctypes.c_int32), ("group_guides", ctypes.c_int32),
-                ("ctas_per_sm", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("ctas_per_sm", ctypes.c_int32), ("split_families", ctypes.c_int32)]
 
 
 class Plan:
@@ -302,12 +304,12 @@ class Plan:
               "bgo_plan_info")
         return {"n_families": nf.value, "n_guides": ng.value}
 
-    def set_tuning(self, chunk_sites=0, group_guides=0, ctas_per_sm=0):
+    def set_tuning(self, chunk_sites=0, group_guides=0, ctas_per_sm=0, split_families=0):
         """Launch parameters of scan modes 2 and 3 (see bgo_plan_set_tuning)."""
-        t = Tuning(int(chunk_sites), int(group_guides), int(ctas_per_sm), 0)
+        t = Tuning(int(chunk_sites), int(group_guides), int(ctas_per_sm), int(split_families))
         check(lib().bgo_plan_set_tuning(self.handle, ctypes.byref(t)), "bgo_plan_set_tuning")
         self.tuning = {"chunk_sites": int(chunk_sites), "group_guides": int(group_guides),
-                       "ctas_per_sm": int(ctas_per_sm)}
+                       "ctas_per_sm": int(ctas_per_sm), "split_families": int(split_families)}
 
     def close(self):
         if self.handle is not None and self.handle.value:
@@ -350,6 +352,16 @@ class Engine:
         check(lib().bgo_scan_collect(self.handle, ptr(keys), keys.size, ctypes.byref(n), stream),
               "bgo_scan_collect")
         return n.value, keys
+
+    def scan_time(self, plan, strands, n_encoded, max_mismatches, mode, reps=2, stream=None):
+        """Fastest of `reps` event-timed scans after one untimed launch (ms)."""
+        arr = (ctypes.c_void_p * len(strands))(*[s.handle.value for s in strands])
+        ne = np.ascontiguousarray(n_encoded, dtype=np.int32)
+        ms = ctypes.c_double()
+        check(lib().bgo_scan_time(self.handle, plan.handle, arr, ptr(ne), len(strands),
+                                  int(max_mismatches), int(mode), int(reps), stream,
+                                  ctypes.byref(ms)), "bgo_scan_time")
+        return ms.value
 
     def hit_count(self, stream=None):
         n = ctypes.c_int64()

@@ -1,0 +1,127 @@
+"""Scan autotuner: picks the scan form and its launch parameters for a plan.
+
+The reference launches one fixed kernel shape (256 threads per block over
+200 Mbp chunks, beguidedoff/cuda_search.py:420-470).  Here the best form
+depends on the plan: the segment index (scan mode 2) wins when each PAM family
+holds few guides per bucket, comparing every guide (mode 1) wins at large
+max_mismatches where K + 1 short segments filter little, and the segment
+masks (mode 3) or per-family launches can win in between.  The tuner times
+each candidate on a sample of the resident genome with CUDA events
+(bgo_scan_time) and keeps the fastest.  Choices are cached by the plan's
+signature: max_mismatches and, per PAM family, the guide count rounded up to
+a power of two.
+
+Candidate parameters: scan mode; tile length (positions per warp chunk,
+``chunk_sites``); guides per mask group (``group_guides``, mode 3); one
+launch per PAM family (``split_families``, mode 2).
+"""
+from dataclasses import dataclass, field
+from typing import Dict, List, Sequence, Tuple
+
+import numpy as np
+
+from . import _native
+
+# (name, mode, (chunk_sites, group_guides, ctas_per_sm, split_families))
+CANDIDATES: Tuple[Tuple[str, int, Tuple[int, int, int, int]], ...] = (
+    ("all-guides", 1, (0, 0, 0, 0)),
+    ("segment-index", 2, (0, 0, 0, 0)),
+    ("segment-index/per-family", 2, (0, 0, 0, 1)),
+    ("segment-masks/2048x128", 3, (2048, 128, 0, 0)),
+    ("segment-masks/1024x128", 3, (1024, 128, 0, 0)),
+    ("segment-masks/2048x64", 3, (2048, 64, 0, 0)),
+)
+INDEXED_MAX_K = 7
+
+
+@dataclass
+class Choice:
+    name: str
+    mode: int
+    tuning: Tuple[int, int, int, int]
+    times_ms: Dict[str, float] = field(default_factory=dict)
+    sample_bp: int = 0
+
+    def as_dict(self):
+        return {"name": self.name, "mode": self.mode,
+                "tuning": dict(zip(("chunk_sites", "group_guides", "ctas_per_sm",
+                                    "split_families"), self.tuning)),
+                "times_ms": {k: round(v, 4) for k, v in self.times_ms.items()},
+                "sample_bp": self.sample_bp}
+
+
+def signature(pams: Sequence[str], max_mismatches: int) -> tuple:
+    """Cache key: K and, per PAM family, the guide count rounded up to a power
+    of two."""
+    counts: Dict[str, int] = {}
+    for p in pams:
+        counts[p.upper()] = counts.get(p.upper(), 0) + 1
+    return (int(max_mismatches),) + tuple(
+        sorted((p, 1 << max(0, int(c - 1).bit_length())) for p, c in counts.items()))
+
+
+def candidates_for(max_mismatches: int, n_families: int) -> List[Tuple[str, int, tuple]]:
+    out = []
+    for name, mode, tune in CANDIDATES:
+        if mode in (2, 3) and max_mismatches > INDEXED_MAX_K:
+            continue
+        if tune[3] and n_families < 2:
+            continue
+        out.append((name, mode, tune))
+    return out
+
+
+class Autotuner:
+    """Times the candidates on the first ``sample_bp`` positions of each
+    strand (a prefix of the host arrays, uploaded once)."""
+
+    def __init__(self, engine, strand_arrays, n_masks, total_bp: int, device: int = 0,
+                 sample_bp: int = 200_000_000, reps: int = 2):
+        self.engine = engine
+        self.reps = reps
+        self.sample_bp = int(min(total_bp, sample_bp))
+        self.device = device
+        self._arrays = strand_arrays
+        self._masks = n_masks
+        self._strands = None
+        self.cache: Dict[tuple, Choice] = {}
+
+    def _sample(self):
+        if self._strands is None:
+            n = self.sample_bp
+            words, nbytes = (n + 15) // 16, (n + 7) // 8
+            self._strands = []
+            for arr, m in zip(self._arrays, self._masks):
+                mm = None if m is None else np.ascontiguousarray(
+                    np.pad(np.asarray(m)[:nbytes], (0, 16)))
+                self._strands.append(_native.Strand(np.ascontiguousarray(arr[:words]), n, mm,
+                                                    self.device))
+        return self._strands
+
+    def choose(self, plan, pams: Sequence[str], max_mismatches: int, stream=None) -> Choice:
+        """The fastest candidate for this plan (cached by signature); the
+        plan's tuning is set to it."""
+        sig = signature(pams, max_mismatches)
+        hit = self.cache.get(sig)
+        if hit is None:
+            strands = self._sample()
+            ne = [0, 3][:len(strands)]
+            n_fam = len({p.upper() for p in pams})
+            times: Dict[str, float] = {}
+            best = None
+            for name, mode, tune in candidates_for(max_mismatches, n_fam):
+                plan.set_tuning(*tune)
+                ms = self.engine.scan_time(plan, strands, ne, max_mismatches, mode,
+                                           self.reps, stream)
+                times[name] = ms
+                if best is None or ms < best[0]:
+                    best = (ms, name, mode, tune)
+            hit = Choice(best[1], best[2], best[3], times, self.sample_bp)
+            self.cache[sig] = hit
+        plan.set_tuning(*hit.tuning)
+        return hit
+
+    def close(self):
+        for s in self._strands or []:
+            s.close()
+        self._strands = None

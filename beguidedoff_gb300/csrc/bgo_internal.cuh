@@ -207,6 +207,8 @@ struct bgo_plan {
     int seed_ok;              // 0: the filter does not apply to this K
     unsigned char *d_seed;    // device block: families | offsets | lists
     bgo::SeedArgs seed;
+    std::vector<bgo::SeedArgs> seed_fam;  // the same index, one family per launch
+    unsigned char *d_seed_fam;            // rebased per-family SeedFam copies
     // segment-mask index for one (max_mismatches, group size) pair
     int mask_k;               // -1000 = not built
     int mask_group;           // guides per group it was built with

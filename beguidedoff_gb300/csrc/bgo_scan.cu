@@ -353,6 +353,7 @@ extern "C" int bgo_plan_create(bgo_engine *engine, const uint64_t *guide_encoded
     pl->h_fams = new (std::nothrow) FamilyDesc[fams.size() + 1];
     pl->h_guides = new (std::nothrow) GuideRec[recs.size() + 1];
     pl->seed_k = -1000;
+    pl->d_seed_fam = nullptr;
     pl->mask_k = -1000;
     pl->mask_group = 0;
     pl->mask_ok = 0;
@@ -390,6 +391,7 @@ extern "C" int bgo_plan_destroy(bgo_plan *pl) {
     delete[] pl->h_fams;
     delete[] pl->h_guides;
     if (pl->d_seed) cudaFree(pl->d_seed);
+    if (pl->d_seed_fam) cudaFree(pl->d_seed_fam);
     if (pl->d_mask) cudaFree(pl->d_mask);
     delete pl;
     return BGO_OK;
@@ -400,9 +402,9 @@ extern "C" int bgo_plan_set_tuning(bgo_plan *pl, const bgo_tuning *t) {
     if ((t->chunk_sites != 0 && t->chunk_sites != 1024 && t->chunk_sites != 2048) ||
         (t->group_guides != 0 && t->group_guides != 32 && t->group_guides != 64 &&
          t->group_guides != 128) ||
-        t->ctas_per_sm < 0) {
+        t->ctas_per_sm < 0 || t->split_families < 0 || t->split_families > 1) {
         set_error("bgo_plan_set_tuning: chunk_sites 1024|2048, group_guides 32|64|128, "
-                  "ctas_per_sm >= 0");
+                  "ctas_per_sm >= 0, split_families 0|1");
         return BGO_ERR_ARG;
     }
     pl->tuning = *t;
@@ -436,11 +438,14 @@ static void fill_strand(StrandDesc &d, const bgo_genome *g, int32_t n_encoded, i
 // guide (mode 1), or a negative BGO_ERR_*.
 static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s) {
     if (pl->seed_k == K) return pl->seed_ok;
-    if (pl->d_seed) {
+    if (pl->d_seed || pl->d_seed_fam) {
         BGO_CUDA(cudaStreamSynchronize(s));
-        cudaFree(pl->d_seed);
+        if (pl->d_seed) cudaFree(pl->d_seed);
+        if (pl->d_seed_fam) cudaFree(pl->d_seed_fam);
         pl->d_seed = nullptr;
+        pl->d_seed_fam = nullptr;
     }
+    pl->seed_fam.clear();
     pl->seed_k = K;
     pl->seed_ok = 0;
     std::vector<SeedFam> sf;
@@ -476,6 +481,36 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
     sa.offsets = reinterpret_cast<const uint32_t *>(pl->d_seed + o_o);
     sa.entry_idx = reinterpret_cast<const uint16_t *>(pl->d_seed + o_i);
     pl->seed = sa;
+    // per-family views of the same index: family f's SeedFam rebased to its
+    // own lists and bucket tables
+    std::vector<SeedFam> rebased(sf);
+    std::vector<SeedArgs> views(sf.size());
+    for (size_t f = 0; f < sf.size(); ++f) {
+        const FamilyDesc &F = pl->h_fams[f];
+        const uint32_t G = (uint32_t)(F.gend - F.gbeg);
+        const uint32_t off0 = sf[f].seg[0].off;
+        const uint32_t off_end =
+            f + 1 < sf.size() ? sf[f + 1].seg[0].off : (uint32_t)offs.size();
+        rebased[f].list_off = 0;
+        for (int j = 0; j < sf[f].nseg; ++j) rebased[f].seg[j].off = sf[f].seg[j].off - off0;
+        SeedArgs v{};
+        v.n_fams = 1;
+        v.n_guides = (int32_t)G;
+        v.n_offsets = (int32_t)(off_end - off0);
+        v.n_lists = (int32_t)((uint32_t)sf[f].nseg * G);
+        v.entries = sa.entries + sf[f].list_off;
+        v.entry_idx = sa.entry_idx + sf[f].list_off;
+        v.offsets = sa.offsets + off0;
+        views[f] = v;
+    }
+    BGO_CUDA(cudaMalloc(&pl->d_seed_fam, sizeof(SeedFam) * (rebased.size() + 1)));
+    BGO_CUDA(cudaMemcpyAsync(pl->d_seed_fam, rebased.data(), sizeof(SeedFam) * rebased.size(),
+                             cudaMemcpyHostToDevice, s));
+    BGO_CUDA(cudaStreamSynchronize(s));
+    engine->h2d_bytes += (int64_t)(sizeof(SeedFam) * rebased.size());
+    for (size_t f = 0; f < views.size(); ++f)
+        views[f].fams = reinterpret_cast<const SeedFam *>(pl->d_seed_fam) + f;
+    pl->seed_fam = views;
     pl->seed_ok = 1;
     return 1;
 }
@@ -612,11 +647,21 @@ extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
         p.n_strands = n_strands;
         p.tiles_total = p.strand[0].n_tiles + (n_strands > 1 ? p.strand[1].n_tiles : 0);
         if (p.tiles_total == 0) return BGO_OK;
-        p.fam_begin = 0;
-        p.fam_end = plan->n_families;
-        const int rc = launch_seed_kernel(p, plan->seed, engine->sm_count, s);
-        if (rc != BGO_OK) return rc;
-        engine->launches++;
+        if (plan->tuning.split_families && plan->n_families > 1) {
+            for (int f = 0; f < plan->n_families; ++f) {
+                p.fam_begin = f;
+                p.fam_end = f + 1;
+                const int rc = launch_seed_kernel(p, plan->seed_fam[(size_t)f], engine->sm_count, s);
+                if (rc != BGO_OK) return rc;
+                engine->launches++;
+            }
+        } else {
+            p.fam_begin = 0;
+            p.fam_end = plan->n_families;
+            const int rc = launch_seed_kernel(p, plan->seed, engine->sm_count, s);
+            if (rc != BGO_OK) return rc;
+            engine->launches++;
+        }
     } else {
         for (int i = 0; i < n_strands; ++i) fill_strand(p.strand[i], strands[i], n_encoded[i], i);
         p.n_strands = n_strands;
@@ -629,6 +674,36 @@ extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
         BGO_CUDA(cudaGetLastError());
         engine->launches++;
     }
+    return BGO_OK;
+}
+
+extern "C" int bgo_scan_time(bgo_engine *engine, const bgo_plan *plan,
+                             const bgo_genome *const *strands, const int32_t *n_encoded,
+                             int32_t n_strands, int32_t max_mismatches, int32_t mode, int32_t reps,
+                             void *stream, double *ms_best) {
+    if (!engine || !ms_best || reps < 1) return BGO_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = bgo_scan_launch(engine, plan, strands, n_encoded, n_strands, max_mismatches, mode, s);
+    if (rc != BGO_OK) return rc;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    BGO_CUDA(cudaEventCreate(&e0));
+    cudaError_t ce = cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int r = 0; r < reps && ce == cudaSuccess && rc == BGO_OK; ++r) {
+        ce = cudaEventRecord(e0, s);
+        if (ce == cudaSuccess)
+            rc = bgo_scan_launch(engine, plan, strands, n_encoded, n_strands, max_mismatches, mode, s);
+        if (ce == cudaSuccess && rc == BGO_OK) ce = cudaEventRecord(e1, s);
+        if (ce == cudaSuccess && rc == BGO_OK) ce = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (ce == cudaSuccess && rc == BGO_OK) ce = cudaEventElapsedTime(&ms, e0, e1);
+        if (ce == cudaSuccess && rc == BGO_OK && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (rc != BGO_OK) return rc;
+    if (ce != cudaSuccess) return cuda_fail(ce, "bgo_scan_time");
+    *ms_best = best;
     return BGO_OK;
 }
 

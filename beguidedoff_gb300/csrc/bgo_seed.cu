@@ -164,12 +164,12 @@ __global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p
         for (int f = p.fam_begin; f < p.fam_end; ++f) {
             const FamilyDesc F = p.fams[f];
             const uint32_t win_off = F.three_prime ? 0u : (uint32_t)F.plen;
-            const int n_tests = sFam[f].n_tests;
+            const int n_tests = sFam[f - p.fam_begin].n_tests;
             uint32_t tsh[kMaxPam], tcd[kMaxPam];
 #pragma unroll
             for (int k = 0; k < kMaxPam; ++k) {
-                tsh[k] = sFam[f].pam_shift[k];
-                tcd[k] = sFam[f].pam_code[k];
+                tsh[k] = sFam[f - p.fam_begin].pam_shift[k];
+                tcd[k] = sFam[f - p.fam_begin].pam_code[k];
             }
             uint32_t pass[kChunkRows];
             int cnt = 0;
@@ -208,11 +208,11 @@ __global__ void __launch_bounds__(kSeedThreads, 3) scan_seed_kernel(ScanParams p
             // the family's bucket tables and entry bases, held in registers
             uint32_t seg_off[S], seg_ent[S];
             {
-                const uint32_t list_off = sFam[f].list_off;
+                const uint32_t list_off = sFam[f - p.fam_begin].list_off;
                 const uint32_t gf = (uint32_t)(F.gend - F.gbeg);
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
-                    seg_off[j] = sFam[f].seg[j].off;
+                    seg_off[j] = sFam[f - p.fam_begin].seg[j].off;
                     seg_ent[j] = list_off + (uint32_t)j * gf;
                 }
             }

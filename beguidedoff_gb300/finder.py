@@ -122,7 +122,7 @@ class beguidedoff:
     def __init__(self, genome_path: str, max_mismatches: int = 4, scoring_method: str = "CCTOP",
                  device: Optional[str] = None, n_top_offtargets: int = 3,
                  results_per_guide: int = 10240, max_results_per_guide: Optional[int] = None,
-                 genome_data: Optional[dict] = None, scan_mode: int = 2,
+                 genome_data: Optional[dict] = None, scan_mode="auto",
                  epilogue: str = "device"):
         if epilogue not in ("device", "host"):
             raise ValueError("epilogue must be 'device' or 'host'")
@@ -135,7 +135,11 @@ class beguidedoff:
         self.n_top_offtargets = n_top_offtargets
         self.results_per_guide = results_per_guide
         self.max_results_per_guide = max_results_per_guide
+        if scan_mode != "auto" and scan_mode not in (0, 1, 2, 3):
+            raise ValueError("scan_mode must be 'auto' or 0..3")
         self.scan_mode = scan_mode
+        self._tuner = None
+        self.last_choice = None
         self.device_index = _device_index(device)
         self.device = f"cuda:{self.device_index}"
         self._init_host(genome_data if genome_data is not None else load_genome(genome_path))
@@ -173,6 +177,8 @@ class beguidedoff:
         self.results_per_guide = results_per_guide
         self.max_results_per_guide = max_results_per_guide
         self.scan_mode = 1
+        self._tuner = None
+        self.last_choice = None
         self.epilogue = "host"
         self.device_index, self.device = -1, "none"
         self._engine, self._strands = None, []
@@ -185,6 +191,9 @@ class beguidedoff:
                 "n_chromosomes": len(self.chrom_names), "chromosomes": self.chrom_names}
 
     def close(self):
+        if getattr(self, "_tuner", None) is not None:
+            self._tuner.close()
+            self._tuner = None
         for s in getattr(self, "_strands", []):
             s.close()
         self._strands = []
@@ -225,13 +234,27 @@ class beguidedoff:
         p3 = np.ones(n, dtype=np.uint8)
         return _native.Plan(self._engine, gv, pm, pl, p3)
 
+    def _mode_for(self, plan, plan_pams: List[str]) -> int:
+        """The scan mode to run: the constructor's, or the autotuner's choice
+        (which also sets the plan's launch tuning)."""
+        if self.scan_mode != "auto":
+            return int(self.scan_mode)
+        if self._tuner is None:
+            from .autotune import Autotuner
+
+            masks = [self._n_mask_fwd, self._n_mask_rc][:len(self._strand_arrays)]
+            self._tuner = Autotuner(self._engine, self._strand_arrays, masks, self.total_bp,
+                                    self.device_index)
+        self.last_choice = self._tuner.choose(plan, plan_pams, self.max_mismatches)
+        return self.last_choice.mode
+
     def _scan(self, plan_seqs: List[str], plan_pams: List[str]) -> np.ndarray:
         """Device scan of both strands; sorted hit keys."""
         plan = self._plan(plan_seqs, plan_pams)
         try:
+            mode = self._mode_for(plan, plan_pams)
             ne = [0, 3][:len(self._strands)]
-            return self._engine.scan(plan, self._strands, ne, self.max_mismatches,
-                                     mode=self.scan_mode)
+            return self._engine.scan(plan, self._strands, ne, self.max_mismatches, mode=mode)
         finally:
             plan.close()
 
@@ -245,12 +268,13 @@ class beguidedoff:
         plan = self._plan([s for s, _ in plan_items], [p for _, p in plan_items])
         try:
             eng = self._engine
+            mode = self._mode_for(plan, [p for _, p in plan_items])
             ne = [0, 3][:len(self._strands)]
-            eng.launch(plan, self._strands, ne, self.max_mismatches, self.scan_mode)
+            eng.launch(plan, self._strands, ne, self.max_mismatches, mode)
             n = eng.hit_count()
             if n > eng.info()["hit_capacity"]:
                 eng.reserve(n)
-                eng.launch(plan, self._strands, ne, self.max_mismatches, self.scan_mode)
+                eng.launch(plan, self._strands, ne, self.max_mismatches, mode)
             pairs = [(int(key_plan[ki]), g, key[2:]) for ki, key in enumerate(keys)
                      for g in mapping[key]]
             inputs = epilogue_inputs(pairs, threshold_rank(count_score_threshold), return_all)

@@ -339,7 +339,14 @@ def bench_ours(args, ws, rank, local):
         nm_pin.append(hb)
     gv, pm, pl, p3 = plan_arrays(guides, pams)
     plan = _native.Plan(f._engine, gv, pm, pl, p3)
-    plan.set_tuning(args.chunk_sites, args.group_guides, args.ctas_per_sm)
+    autotune = None
+    if args.mode == "auto":
+        t0 = time.perf_counter()
+        f._mode_for(plan, pams)
+        autotune = dict(f.last_choice.as_dict(), seconds=time.perf_counter() - t0)
+        args.mode = f.last_choice.mode
+    else:
+        plan.set_tuning(args.chunk_sites, args.group_guides, args.ctas_per_sm)
     if dense:
         editors = [DENSE_EDITORS[i % 3] for i in range(len(guides))]
     else:
@@ -509,6 +516,7 @@ def bench_ours(args, ws, rank, local):
                     "rows": len(table), "launches": e2e_launches // args.steps},
             "gpu_launches": launches,
             "tuning": getattr(plan, "tuning", None),
+            "autotune": autotune,
             "epilogue": epi,
             "graph": graph is not None,
             "plain_form": plain,
@@ -532,7 +540,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", type=int, default=2, choices=[0, 1, 2, 3])
+    ap.add_argument("--mode", default="auto", choices=["auto", "0", "1", "2", "3"],
+                    help="scan form: auto = the project autotuner's choice")
     ap.add_argument("--chunk-sites", type=int, default=0, help="modes 2/3 tile length (0 = default)")
     ap.add_argument("--group-guides", type=int, default=0, help="mode 3 guides per group")
     ap.add_argument("--ctas-per-sm", type=int, default=0)
@@ -546,6 +555,8 @@ def main():
                     help="plain: 100 NGG guides, <=4 mm; mixed: 400 mixed-PAM guides, <=5 mm; "
                          "dense: repeat-family genome, 1000 mixed guides, <=6 mm")
     args = ap.parse_args()
+    if args.mode != "auto":
+        args.mode = int(args.mode)
     if args.warmup < 3:
         args.warmup = 3
     if args.config in ("mixed", "dense"):

@@ -141,6 +141,9 @@ int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
  *                 or 128; a family larger than this is cut into several groups
  *   ctas_per_sm   cap on resident CTAs per SM for the grid size (0 = the
  *                 occupancy maximum)
+ *   split_families  mode 2: one launch per PAM family, each holding only its
+ *                 family's index in shared memory (higher occupancy when the
+ *                 combined index is large), instead of one launch for all
  * Changing group_guides rebuilds the mask index at the next launch.  No
  * reference counterpart: the reference fixes 256 threads x 200 Mbp chunks.
  */
@@ -148,9 +151,18 @@ typedef struct bgo_tuning {
     int32_t chunk_sites;
     int32_t group_guides;
     int32_t ctas_per_sm;
-    int32_t reserved;
+    int32_t split_families;
 } bgo_tuning;
 int bgo_plan_set_tuning(bgo_plan *plan, const bgo_tuning *tuning);
+
+/*
+ * Times the scan: one untimed launch, then `reps` launches each bracketed by
+ * CUDA events on `stream`; *ms_best = the fastest.  The autotuner's
+ * measurement.  No reference counterpart.
+ */
+int bgo_scan_time(bgo_engine *engine, const bgo_plan *plan, const bgo_genome *const *strands,
+                  const int32_t *n_encoded, int32_t n_strands, int32_t max_mismatches,
+                  int32_t mode, int32_t reps, void *stream, double *ms_best);
 
 /*
  * The same scan as bgo_scan_launch, captured once into a CUDA graph and

@@ -154,6 +154,34 @@ def test_random_mixed_pam_keys_equal_oracle(seed):
         f.close()
 
 
+def test_autotuned_scan_equals_oracle():
+    """scan_mode='auto': the tuner times every candidate on the genome and the
+    chosen form (with its tuning, including per-family launches) returns the
+    oracle's keys."""
+    genome, rng = _random_genome(77, [900_000, 650_000])
+    seqs, pams = [], []
+    for i in range(60):
+        s = "".join(rng.choice(list("ACGT"), 20))
+        pam = MIXED_PAMS[i % 5]
+        _plant(genome, rng, s, pam, 5, 5)
+        seqs.append(s)
+        pams.append(pam)
+    exp = oracle_keys(genome, seqs, pams, 5)
+    f = beguidedoff(None, max_mismatches=5, genome_data=genome)
+    try:
+        assert f.scan_mode == "auto"
+        got = f._scan(seqs, pams)
+        assert np.array_equal(got, exp)
+        ch = f.last_choice
+        assert ch is not None and len(ch.times_ms) >= 5 and ch.mode in (1, 2, 3)
+        plan = f._plan(seqs, pams)
+        plan.set_tuning(0, 0, 0, 1)   # one launch per family
+        assert np.array_equal(f._engine.scan(plan, f._strands, [0, 3], 5, 2), exp)
+        plan.close()
+    finally:
+        f.close()
+
+
 @pytest.mark.parametrize("k", [0, 1, 2, 3, 6, 7])
 def test_indexed_modes_every_k_equal_oracle(k):
     """Segment index (mode 2) and segment masks (mode 3) at every segment
@@ -171,7 +199,7 @@ def test_indexed_modes_every_k_equal_oracle(k):
     try:
         plan = f._plan(seqs, pams)
         tunings = [(0, 0, 0), (1024, 32, 0), (2048, 64, 2), (1024, 128, 1)]
-        for mode, tune in [(2, (0, 0, 0))] + [(3, t) for t in tunings]:
+        for mode, tune in [(2, (0, 0, 0)), (2, (0, 0, 0, 1))] + [(3, t) for t in tunings]:
             plan.set_tuning(*tune)
             got = f._engine.scan(plan, f._strands, [0, 3], k, mode)
             assert got.size == exp.size and np.array_equal(got, exp), (mode, tune)
