@@ -27,7 +27,8 @@ EXPORTED = [
     "bgo_engine_info", "bgo_synth_genome", "bgo_probe_int_throughput", "bgo_scan_stats",
     "bgo_scan_noalloc", "bgo_graph_create", "bgo_graph_launch", "bgo_graph_destroy",
     "bgo_epilogue_run", "bgo_synth_genome_repeats", "bgo_engine_transfer",
-    "bgo_plan_set_tuning", "bgo_epilogue_fetch", "bgo_scan_time",
+    "bgo_plan_set_tuning", "bgo_epilogue_fetch", "bgo_scan_time", "bgo_stream_create",
+    "bgo_stream_destroy",
 ]
 
 INPUT_ROW_DTYPE = np.dtype([("plan_row", "<i4"), ("window_mask", "<u4"), ("target_base", "<i4"),
@@ -83,6 +84,8 @@ _SIGS = {
     "bgo_epilogue_run": ([_P, _P, _P, _I32, _P, _I32, _P, _P, _P, _I32, _P, _I32, _P, _P, _P,
                           ctypes.POINTER(_I64), _P], ctypes.c_int),
     "bgo_epilogue_fetch": ([_P, _P, _I64, _P], ctypes.c_int),
+    "bgo_stream_create": ([ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "bgo_stream_destroy": ([_P], ctypes.c_int),
     "bgo_scan_time": ([_P, _P, _P, _P, _I32, _I32, _I32, _I32, _P,
                        ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "bgo_scan_noalloc": ([_P, _P, _I32, _P, _P, _P, _P, _I32, _I32, _P, _I64,
@@ -263,6 +266,27 @@ class Strand:
     def close(self):
         if self.handle is not None and self.handle.value:
             lib().bgo_genome_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Stream:
+    """A non-blocking CUDA stream (bgo_stream_create); pass ``.handle`` as the
+    stream argument."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        check(lib().bgo_stream_create(int(device), ctypes.byref(h)), "bgo_stream_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle is not None and self.handle.value:
+            lib().bgo_stream_destroy(self.handle)
         self.handle = None
 
     def __del__(self):

@@ -76,8 +76,9 @@ class Autotuner:
     strand (a prefix of the host arrays, uploaded once)."""
 
     def __init__(self, engine, strand_arrays, n_masks, total_bp: int, device: int = 0,
-                 sample_bp: int = 200_000_000, reps: int = 2):
+                 sample_bp: int = 200_000_000, reps: int = 2, coarse: bool = False):
         self.engine = engine
+        self.coarse = coarse   # one choice per max_mismatches (serving)
         self.reps = reps
         self.sample_bp = int(min(total_bp, sample_bp))
         self.device = device
@@ -101,7 +102,7 @@ class Autotuner:
     def choose(self, plan, pams: Sequence[str], max_mismatches: int, stream=None) -> Choice:
         """The fastest candidate for this plan (cached by signature); the
         plan's tuning is set to it."""
-        sig = signature(pams, max_mismatches)
+        sig = (int(max_mismatches),) if self.coarse else signature(pams, max_mismatches)
         hit = self.cache.get(sig)
         if hit is None:
             strands = self._sample()

@@ -53,3 +53,19 @@ extern "C" int bgo_host_free(void *ptr) {
     if (ptr) BGO_CUDA(cudaFreeHost(ptr));
     return BGO_OK;
 }
+
+extern "C" int bgo_stream_create(int device, void **stream) {
+    if (!stream) return BGO_ERR_ARG;
+    *stream = nullptr;
+    BGO_CUDA(cudaSetDevice(device));
+    cudaStream_t s = nullptr;
+    BGO_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    *stream = (void *)s;
+    return BGO_OK;
+}
+
+extern "C" int bgo_stream_destroy(void *stream) {
+    if (!stream) return BGO_OK;
+    BGO_CUDA(cudaStreamDestroy((cudaStream_t)stream));
+    return BGO_OK;
+}

@@ -23,6 +23,7 @@ Reference behaviours kept on purpose (each pinned by tests/golden):
     (here: the genome-order prefix) and a warning gives the exact count.
 """
 import logging
+import threading
 from collections import defaultdict
 from pathlib import Path
 from typing import Dict, List, Optional, Tuple
@@ -139,7 +140,9 @@ class beguidedoff:
             raise ValueError("scan_mode must be 'auto' or 0..3")
         self.scan_mode = scan_mode
         self._tuner = None
+        self._tuner_lock = threading.Lock()
         self.last_choice = None
+        self.last_batch = None
         self.device_index = _device_index(device)
         self.device = f"cuda:{self.device_index}"
         self._init_host(genome_data if genome_data is not None else load_genome(genome_path))
@@ -178,7 +181,9 @@ class beguidedoff:
         self.max_results_per_guide = max_results_per_guide
         self.scan_mode = 1
         self._tuner = None
+        self._tuner_lock = threading.Lock()
         self.last_choice = None
+        self.last_batch = None
         self.epilogue = "host"
         self.device_index, self.device = -1, "none"
         self._engine, self._strands = None, []
@@ -223,7 +228,7 @@ class beguidedoff:
             mapping[(g.guide_seq, g.pam, ci, lp, st)].append(g)
         return list(mapping), mapping
 
-    def _plan(self, plan_seqs: List[str], plan_pams: List[str]):
+    def _plan(self, plan_seqs: List[str], plan_pams: List[str], engine=None, stream=None):
         n = len(plan_seqs)
         gv = np.array([encode_guide_64bit(encode_dna(s)[:20]) for s in plan_seqs],
                       dtype=np.uint64)
@@ -232,21 +237,24 @@ class beguidedoff:
             pm[i] = encode_pam_mask(pam)
         pl = np.array([len(p) for p in plan_pams], dtype=np.uint8)
         p3 = np.ones(n, dtype=np.uint8)
-        return _native.Plan(self._engine, gv, pm, pl, p3)
+        return _native.Plan(engine or self._engine, gv, pm, pl, p3, stream)
 
-    def _mode_for(self, plan, plan_pams: List[str]) -> int:
+    def _mode_for(self, plan, plan_pams: List[str], max_mismatches: Optional[int] = None) -> int:
         """The scan mode to run: the constructor's, or the autotuner's choice
         (which also sets the plan's launch tuning)."""
         if self.scan_mode != "auto":
             return int(self.scan_mode)
-        if self._tuner is None:
-            from .autotune import Autotuner
+        k = self.max_mismatches if max_mismatches is None else max_mismatches
+        with self._tuner_lock:
+            if self._tuner is None:
+                from .autotune import Autotuner
 
-            masks = [self._n_mask_fwd, self._n_mask_rc][:len(self._strand_arrays)]
-            self._tuner = Autotuner(self._engine, self._strand_arrays, masks, self.total_bp,
-                                    self.device_index)
-        self.last_choice = self._tuner.choose(plan, plan_pams, self.max_mismatches)
-        return self.last_choice.mode
+                masks = [self._n_mask_fwd, self._n_mask_rc][:len(self._strand_arrays)]
+                self._tuner = Autotuner(self._engine, self._strand_arrays, masks, self.total_bp,
+                                        self.device_index,
+                                        coarse=getattr(self, "tune_per_k", False))
+            self.last_choice = self._tuner.choose(plan, plan_pams, k)
+            return self.last_choice.mode
 
     def _scan(self, plan_seqs: List[str], plan_pams: List[str]) -> np.ndarray:
         """Device scan of both strands; sorted hit keys."""
@@ -258,47 +266,106 @@ class beguidedoff:
         finally:
             plan.close()
 
-    def _search_device(self, keys, key_plan, plan_items, mapping, guides, return_all,
-                       count_score_threshold, log):
-        """Scan + device epilogue; the host only sorts each row's top-N
-        candidates.  Returns None when the host path must run instead
-        (a strand hit limit is reached, or an editor type is unknown)."""
+    def _prepare(self, guides: List[GuideInput]):
+        """Checks of the reference's search() and the dedup to scan keys."""
+        if not guides:
+            raise ValueError("No guides provided")
+        for g in guides:
+            if g.pam_position.lower() != "3prime":
+                raise ValueError(f"Guide {g.guide_id} has pam_position '{g.pam_position}'. "
+                                 f"Only 3prime PAM is supported.")
+        return self._deduplicate_guides(guides)
+
+    def _run_batch(self, reqs: List[dict], max_mismatches: int, engine=None, stream=None,
+                   log=None, info: Optional[dict] = None) -> List[object]:
+        """One plan, one scan and one device epilogue for several searches with
+        the same max_mismatches.  Each request dict holds ``keys``,
+        ``mapping``, ``guides``, ``return_all`` and ``count_score_threshold``;
+        its input rows, options and assembly stay its own, so its table is the
+        one search() returns for it alone.  Returns a table or an exception
+        per request."""
         from .scoring import score_ranks, threshold_rank
 
-        plan = self._plan([s for s, _ in plan_items], [p for _, p in plan_items])
+        eng = engine or self._engine
+        log = log if log is not None else _LOGGER
+        plan_index: Dict[tuple, int] = {}
+        for r in reqs:
+            r["key_plan"] = np.array([plan_index.setdefault((k[0], k[1]), len(plan_index))
+                                      for k in r["keys"]], dtype=np.int64)
+        plan_items = list(plan_index)
+        pams = [p for _, p in plan_items]
+        plan = self._plan([s for s, _ in plan_items], pams, eng, stream)
         try:
-            eng = self._engine
-            mode = self._mode_for(plan, [p for _, p in plan_items])
+            mode = self._mode_for(plan, pams, max_mismatches)
             ne = [0, 3][:len(self._strands)]
-            eng.launch(plan, self._strands, ne, self.max_mismatches, mode)
-            n = eng.hit_count()
+            eng.launch(plan, self._strands, ne, max_mismatches, mode, stream)
+            n = eng.hit_count(stream)
             if n > eng.info()["hit_capacity"]:
                 eng.reserve(n)
-                eng.launch(plan, self._strands, ne, self.max_mismatches, mode)
-            pairs = [(int(key_plan[ki]), g, key[2:]) for ki, key in enumerate(keys)
-                     for g in mapping[key]]
-            inputs = epilogue_inputs(pairs, threshold_rank(count_score_threshold), return_all)
-            if inputs is None:
-                return None
-            owners = [g.guide_id for _, g, _ in pairs]
-            rank_table, _ = score_ranks()
-            below, groups, _, recs = eng.epilogue(
-                plan, self._strands, inputs, self.chrom_offsets, self.chrom_lengths,
-                self._chrom_rank, rank_table, self.n_top_offtargets)
+                eng.launch(plan, self._strands, ne, max_mismatches, mode, stream)
+            self.last_batch = {"hits": n, "plan_rows": len(plan_items), "mode": mode}
+            if info is not None:
+                info.update(self.last_batch)
+            parts, owners, spans, errs = [], [], [], []
+            n_rows = 0
+            for r in reqs:
+                pairs = [(int(r["key_plan"][ki]), g, key[2:]) for ki, key in enumerate(r["keys"])
+                         for g in r["mapping"][key]]
+                try:
+                    rows = epilogue_inputs(pairs, threshold_rank(r["count_score_threshold"]),
+                                           r["return_all"])
+                except Exception as exc:  # the host path raises the same error
+                    rows = None
+                    errs.append(exc)
+                else:
+                    errs.append(None)
+                if rows is None:   # unknown editor or bad window: host path
+                    spans.append(None)
+                    owners.append(None)
+                    continue
+                spans.append((n_rows, len(pairs)))
+                n_rows += len(pairs)
+                parts.append(rows)
+                owners.append([g.guide_id for _, g, _ in pairs])
+            full = None
+            if parts:
+                rank_table, _ = score_ranks()
+                below, groups, counts, recs = eng.epilogue(
+                    plan, self._strands, np.concatenate(parts), self.chrom_offsets,
+                    self.chrom_lengths, self._chrom_rank, rank_table, self.n_top_offtargets,
+                    stream)
+                rec_off = np.concatenate([[0], np.cumsum(counts)])
+            out = []
+            for i, r in enumerate(reqs):
+                try:
+                    if errs[i] is not None:
+                        raise errs[i]
+                    pre = None
+                    if spans[i] is not None:
+                        counts_k = groups[r["key_plan"]]
+                        limit = self._limits(counts_k, r["keys"], log)
+                        if not (counts_k.max(axis=1) > limit).any():
+                            r0, nr = spans[i]
+                            below_by_id: Dict[str, int] = defaultdict(int)
+                            for gid, b in zip(owners[i], below[r0:r0 + nr].tolist()):
+                                below_by_id[gid] += b
+                            hit_keys = np.unique(recs["key"][rec_off[r0]:rec_off[r0 + nr]])
+                            pre = (limit, below_by_id if r["count_score_threshold"] is not None
+                                   else None)
+                    if pre is None:
+                        # a strand hit limit is reached (the genome-order prefix
+                        # of every strand is needed) or an editor type is unknown
+                        if full is None:
+                            _, full = eng.collect(stream)
+                        hit_keys = full
+                    out.append(self._assemble(hit_keys, r["keys"], r["key_plan"], plan_items,
+                                              r["mapping"], r["guides"], r["return_all"],
+                                              r["count_score_threshold"], log, precomputed=pre))
+                except Exception as exc:  # reported to that request only
+                    out.append(exc)
+            return out
         finally:
             plan.close()
-        counts_k = groups[key_plan]
-        limit = self._limits(counts_k, keys, log)
-        if (counts_k.max(axis=1) > limit).any():
-            return None  # truncation needs the genome-order prefix of every strand
-        below_by_id: Dict[str, int] = defaultdict(int)
-        for gid, b in zip(owners, below.tolist()):
-            below_by_id[gid] += b
-        subset = np.unique(recs["key"])
-        return self._assemble(subset, keys, key_plan, plan_items, mapping, guides, return_all,
-                              count_score_threshold, log,
-                              precomputed=(limit, below_by_id if count_score_threshold is not None
-                                           else None))
 
     def _limits(self, counts2: np.ndarray, keys, log) -> np.ndarray:
         """Per scan key the per-strand number of hits kept, with the warnings
@@ -339,30 +406,27 @@ class beguidedoff:
             raise ValueError("Exactly one of input_file or guides must be provided")
         if input_file is not None:
             guides = load_guides_from_tsv(input_file, presets_path=presets_path or _PROFILES)
-        if not guides:
-            raise ValueError("No guides provided")
         log = logger if logger is not None else _LOGGER
-        for g in guides:
-            if g.pam_position.lower() != "3prime":
-                raise ValueError(f"Guide {g.guide_id} has pam_position '{g.pam_position}'. "
-                                 f"Only 3prime PAM is supported.")
-        keys, mapping = self._deduplicate_guides(guides)
+        keys, mapping = self._prepare(guides)
         if verbose:
             log.info("Guides after deduplication: %d (from %d input rows)", len(keys),
                      len(guides))
             log.info("Running GPU search on %s ...", self.device)
-        # one plan row per distinct (seq, pam); scan keys that differ only in
-        # their on-target share it
-        plan_index: Dict[tuple, int] = {}
-        key_plan = np.empty(len(keys), dtype=np.int64)
-        for i, k in enumerate(keys):
-            key_plan[i] = plan_index.setdefault((k[0], k[1]), len(plan_index))
-        plan_items = list(plan_index)
-        table = None
         if self.epilogue == "device":
-            table = self._search_device(keys, key_plan, plan_items, mapping, guides, return_all,
-                                        count_score_threshold, log)
-        if table is None:
+            table = self._run_batch([{"keys": keys, "mapping": mapping, "guides": guides,
+                                      "return_all": return_all,
+                                      "count_score_threshold": count_score_threshold}],
+                                    self.max_mismatches, log=log)[0]
+            if isinstance(table, Exception):
+                raise table
+        else:
+            # one plan row per distinct (seq, pam); scan keys that differ only
+            # in their on-target share it
+            plan_index: Dict[tuple, int] = {}
+            key_plan = np.empty(len(keys), dtype=np.int64)
+            for i, k in enumerate(keys):
+                key_plan[i] = plan_index.setdefault((k[0], k[1]), len(plan_index))
+            plan_items = list(plan_index)
             hit_keys = self._scan([s for s, _ in plan_items], [p for _, p in plan_items])
             table = self._assemble(hit_keys, keys, key_plan, plan_items, mapping, guides,
                                    return_all, count_score_threshold, log)

@@ -534,6 +534,148 @@ def bench_ours(args, ws, rank, local):
         b.close()
 
 
+def serve_trace(rate, duration, seed=11):
+    """Seeded request trace of the serving config: Poisson arrivals at `rate`
+    per second for `duration` seconds; each request 1-500 guides (log-uniform)
+    with PAM family and editor drawn as in the batched config, max_mismatches
+    uniform in 3..5."""
+    from beguidedoff_gb300.types import GuideInput
+
+    rng = np.random.default_rng(seed)
+    fams = [p for p, _ in MIXED_FAMILIES]
+    probs = np.array([f for _, f in MIXED_FAMILIES])
+    t, out = 0.0, []
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t > duration:
+            return out
+        n = int(np.exp(rng.uniform(0, np.log(500))))
+        k = int(rng.integers(3, 6))
+        guides = []
+        for j in range(n):
+            ed = ("ABE", 4, 8, "ABE8e") if rng.random() < 0.5 else ("CBE", 4, 8, "TadCBEd")
+            guides.append(GuideInput(f"g{j}", "".join(rng.choice(list("ACGT"), 20)),
+                                     fams[int(rng.choice(len(fams), p=probs))], "3prime",
+                                     ed[1], ed[2], ed[0], base_editor=ed[3]))
+        out.append((t, guides, k))
+
+
+def _latency_stats(lat, wall, n_guides, comps):
+    lat = np.sort(np.asarray(lat))
+    return {"requests": int(lat.size), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+            "p99_ms": 1e3 * float(np.percentile(lat, 99)), "mean_ms": 1e3 * float(lat.mean()),
+            "max_ms": 1e3 * float(lat.max()), "wall_s": wall,
+            "requests_per_s": lat.size / wall, "guides_per_s": n_guides / wall,
+            "cmp_per_s": comps / wall}
+
+
+def _table_rows(t):
+    return [dict(r) for r in t.rows()] if hasattr(t, "rows") else t.to_dict("records")
+
+
+def bench_serve(args, ws, rank, local):
+    """Serving loop: the same request trace through the continuous-batching
+    server and through serial per-request plain launches (scan mode 0, one
+    request at a time in arrival order, each waiting for the previous one)."""
+    from beguidedoff_gb300 import _native, build
+    from beguidedoff_gb300.finder import beguidedoff
+    from beguidedoff_gb300.serving import SearchServer
+
+    build.build()
+    lens, blocks, _ = make_workload(args.genome_bp, 1)
+    total = int(lens.sum())
+    genome = _native.synth_genome(7, lens, blocks, thresholds=(76, 128, 180), device=local)
+    trace = serve_trace(args.rate, args.duration)
+    warm = serve_trace(args.rate, min(3.0, args.duration), seed=99)
+    n_guides = sum(len(g) for _, g, _ in trace)
+    comps = n_guides * 2 * (total - 26)
+
+    def replay_server(srv, items):
+        t0 = time.perf_counter()
+        done_at = {}
+        futs = []
+        for i, (t, guides, k) in enumerate(items):
+            d = t0 + t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            fut = srv.submit(guides, k)
+            fut.add_done_callback(lambda f, i=i: done_at.__setitem__(i, time.perf_counter()))
+            futs.append(fut)
+        res = [f.result() for f in futs]
+        wall = time.perf_counter() - t0
+        lat = [done_at[i] - (t0 + items[i][0]) for i in range(len(items))]
+        return lat, wall, res
+
+    def replay_serial(fin, items):
+        t0 = time.perf_counter()
+        lat, res = [], []
+        for t, guides, k in items:
+            d = t0 + t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            fin.max_mismatches = k
+            res.append(fin.search(guides=guides, verbose=False))
+            lat.append(time.perf_counter() - (t0 + t))
+        return lat, time.perf_counter() - t0, res
+
+    clocks = ClockSampler(local).start()
+    srv = SearchServer(genome_data=genome, device=f"cuda:{local}", n_slots=args.slots,
+                       memory_bytes=args.serve_memory << 30, max_batch_guides=args.batch_guides)
+    replay_server(srv, warm)
+    b0 = len(srv.batches)
+    x0 = [e.transfer() for e, _ in srv.slots]
+    lat_b, wall_b, res_b = replay_server(srv, trace)
+    x1 = [e.transfer() for e, _ in srv.slots]
+    batches = srv.batches[b0:]
+    launches = sum(e.launch_count() for e, _ in srv.slots)
+    srv_stats = _latency_stats(lat_b, wall_b, n_guides, comps)
+    srv_stats.update({
+        "batches": len(batches),
+        "requests_per_batch": float(np.mean([b["requests"] for b in batches])),
+        "guides_per_batch": float(np.mean([b["guides"] for b in batches])),
+        "slots": args.slots, "memory_gb": args.serve_memory,
+        "max_batch_guides": args.batch_guides,
+        "autotune": {str(k[0]): v.name for k, v in
+                     (srv.finder._tuner.cache.items() if srv.finder._tuner else [])}})
+    srv.close()
+    base = beguidedoff(None, max_mismatches=4, genome_data=genome, device=f"cuda:{local}",
+                       scan_mode=0)
+    replay_serial(base, warm[:4])
+    lat_s, wall_s, res_s = replay_serial(base, trace)
+    base.close()
+    clk = clocks.stop()
+    ser_stats = _latency_stats(lat_s, wall_s, n_guides, comps)
+    same = all(_table_rows(a) == _table_rows(b) for a, b in zip(res_b, res_s))
+    h2d = sum(b["h2d"] - a["h2d"] for a, b in zip(x0, x1))
+    d2h = sum(b["d2h"] - a["d2h"] for a, b in zip(x0, x1))
+    out = {
+        "metric": METRIC, "value": srv_stats["cmp_per_s"], "unit": UNIT, "n_gpus": ws,
+        "steps": len(trace), "warmup": len(warm), "ms_per_step": srv_stats["mean_ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic",
+        "config": {"workload": (f"serving loop: synthetic {total / 1e9:.2f} Gbp resident, Poisson "
+                                f"arrivals at {args.rate} req/s for {args.duration} s, 1-500 "
+                                f"guides per request (log-uniform), PAM families and editors as "
+                                f"the batched config, max_mismatches 3-5; a step = one request"),
+                   "genome_bp": total, "requests": len(trace), "guides": n_guides,
+                   "rate_per_s": args.rate, "duration_s": args.duration,
+                   "l2": "inputs larger than L2 (bit planes of both strands ~2.3 GB)"},
+        "serving": srv_stats, "serial_plain": ser_stats,
+        "p50_speedup": ser_stats["p50_ms"] / srv_stats["p50_ms"],
+        "p99_speedup": ser_stats["p99_ms"] / srv_stats["p99_ms"],
+        "results_identical": same,
+        "e2e": {"value": srv_stats["cmp_per_s"], "unit": UNIT,
+                "h2d_bytes_per_step": h2d // max(1, len(trace)),
+                "d2h_bytes_per_step": d2h // max(1, len(trace)),
+                "note": "the genome stays resident; per request: guides, plan and epilogue "
+                        "inputs up, epilogue results down"},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -551,7 +693,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
-    ap.add_argument("--config", default="plain", choices=["plain", "mixed", "dense"],
+    ap.add_argument("--rate", type=float, default=20.0, help="serve: requests per second")
+    ap.add_argument("--duration", type=float, default=15.0, help="serve: trace seconds")
+    ap.add_argument("--slots", type=int, default=2, help="serve: concurrent batches")
+    ap.add_argument("--serve-memory", type=int, default=16, help="serve: output-buffer GB")
+    ap.add_argument("--batch-guides", type=int, default=2048, help="serve: guides per batch")
+    ap.add_argument("--config", default="plain", choices=["plain", "mixed", "dense", "serve"],
                     help="plain: 100 NGG guides, <=4 mm; mixed: 400 mixed-PAM guides, <=5 mm; "
                          "dense: repeat-family genome, 1000 mixed guides, <=6 mm")
     args = ap.parse_args()
@@ -567,6 +714,8 @@ def main():
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         bench_reference(args, ws, rank)
+    elif args.config == "serve":
+        bench_serve(args, ws, rank, local)
     else:
         bench_ours(args, ws, rank, local)
     if ws > 1:

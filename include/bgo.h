@@ -237,6 +237,12 @@ int bgo_epilogue_run(bgo_engine *engine, const bgo_plan *plan, const bgo_genome 
 /* Copies the records of the last bgo_epilogue_run (capacity >= its n_records). */
 int bgo_epilogue_fetch(bgo_engine *engine, bgo_record *records, int64_t capacity, void *stream);
 
+/* A non-blocking CUDA stream on `device` (no implicit synchronisation with
+ * the legacy default stream), for callers without a CUDA runtime of their own:
+ * one per concurrent engine lets searches overlap on the device. */
+int bgo_stream_create(int device, void **stream);
+int bgo_stream_destroy(void *stream);
+
 /* Grows the engine's device hit buffer to at least `n_hits` keys. */
 int bgo_engine_reserve(bgo_engine *engine, int64_t n_hits);
 
