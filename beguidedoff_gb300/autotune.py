@@ -60,6 +60,16 @@ def signature(pams: Sequence[str], max_mismatches: int) -> tuple:
         sorted((p, 1 << max(0, int(c - 1).bit_length())) for p, c in counts.items()))
 
 
+SIZE_CLASSES = (16, 64, 256, 1024)
+
+
+def coarse_signature(n_guides: int, max_mismatches: int) -> tuple:
+    """Cache key for plans that mix families freely (serving batches): K and
+    a size class of the guide count (<= 16, <= 64, <= 256, <= 1024, more)."""
+    cls = next((i for i, c in enumerate(SIZE_CLASSES) if n_guides <= c), len(SIZE_CLASSES))
+    return (int(max_mismatches), cls)
+
+
 def candidates_for(max_mismatches: int, n_families: int) -> List[Tuple[str, int, tuple]]:
     out = []
     for name, mode, tune in CANDIDATES:
@@ -78,7 +88,7 @@ class Autotuner:
     def __init__(self, engine, strand_arrays, n_masks, total_bp: int, device: int = 0,
                  sample_bp: int = 200_000_000, reps: int = 2, coarse: bool = False):
         self.engine = engine
-        self.coarse = coarse   # one choice per max_mismatches (serving)
+        self.coarse = coarse   # one choice per (max_mismatches, size class): serving
         self.reps = reps
         self.sample_bp = int(min(total_bp, sample_bp))
         self.device = device
@@ -102,7 +112,8 @@ class Autotuner:
     def choose(self, plan, pams: Sequence[str], max_mismatches: int, stream=None) -> Choice:
         """The fastest candidate for this plan (cached by signature); the
         plan's tuning is set to it."""
-        sig = (int(max_mismatches),) if self.coarse else signature(pams, max_mismatches)
+        sig = coarse_signature(len(pams), max_mismatches) if self.coarse else \
+            signature(pams, max_mismatches)
         hit = self.cache.get(sig)
         if hit is None:
             strands = self._sample()

@@ -24,6 +24,7 @@ Reference behaviours kept on purpose (each pinned by tests/golden):
 """
 import logging
 import threading
+import time
 from collections import defaultdict
 from pathlib import Path
 from typing import Dict, List, Optional, Tuple
@@ -294,16 +295,20 @@ class beguidedoff:
                                       for k in r["keys"]], dtype=np.int64)
         plan_items = list(plan_index)
         pams = [p for _, p in plan_items]
+        t0 = time.perf_counter()
         plan = self._plan([s for s, _ in plan_items], pams, eng, stream)
         try:
             mode = self._mode_for(plan, pams, max_mismatches)
+            t1 = time.perf_counter()
             ne = [0, 3][:len(self._strands)]
             eng.launch(plan, self._strands, ne, max_mismatches, mode, stream)
             n = eng.hit_count(stream)
             if n > eng.info()["hit_capacity"]:
                 eng.reserve(n)
                 eng.launch(plan, self._strands, ne, max_mismatches, mode, stream)
-            self.last_batch = {"hits": n, "plan_rows": len(plan_items), "mode": mode}
+            t2 = time.perf_counter()
+            self.last_batch = {"hits": n, "plan_rows": len(plan_items), "mode": mode,
+                               "plan_s": t1 - t0, "scan_s": t2 - t1}
             if info is not None:
                 info.update(self.last_batch)
             parts, owners, spans, errs = [], [], [], []
@@ -335,6 +340,7 @@ class beguidedoff:
                     self.chrom_lengths, self._chrom_rank, rank_table, self.n_top_offtargets,
                     stream)
                 rec_off = np.concatenate([[0], np.cumsum(counts)])
+            t3 = time.perf_counter()
             out = []
             for i, r in enumerate(reqs):
                 try:
@@ -363,6 +369,9 @@ class beguidedoff:
                                               r["count_score_threshold"], log, precomputed=pre))
                 except Exception as exc:  # reported to that request only
                     out.append(exc)
+            if info is not None:
+                info["epilogue_s"] = (t3 - t2) if parts else 0.0
+                info["assemble_s"] = time.perf_counter() - (t3 if parts else t2)
             return out
         finally:
             plan.close()

@@ -176,6 +176,29 @@ class SearchServer:
         for w in self._workers:
             w.start()
 
+    def warmup(self, max_mismatches=(3, 4, 5), pams=("NGG", "NG", "NNGRRT", "NNNRRT", "NRN"),
+               sizes=(8, 48, 200, 800, 1600), seed: int = 0) -> dict:
+        """Runs the autotuner for every (max_mismatches, size class) on random
+        guides cycling through `pams`, so that no request pays for tuning."""
+        import numpy as np
+
+        rng = np.random.default_rng(seed)
+        f = self.finder
+        if f.scan_mode != "auto":
+            return {}
+        out = {}
+        for k in max_mismatches:
+            for n in sizes:
+                seqs = ["".join(rng.choice(list("ACGT"), 20)) for _ in range(n)]
+                plan_pams = [pams[i % len(pams)] for i in range(n)]
+                plan = f._plan(seqs, plan_pams)
+                try:
+                    f._mode_for(plan, plan_pams, k)
+                    out[(k, n)] = f.last_choice.name
+                finally:
+                    plan.close()
+        return out
+
     def submit(self, guides: List[GuideInput], max_mismatches: int = 4, return_all: bool = False,
                count_score_threshold: Optional[float] = None) -> Future:
         with self._lock:
@@ -208,12 +231,15 @@ class SearchServer:
                              "return_all": r.return_all,
                              "count_score_threshold": r.count_score_threshold})
             hits = None
+            times: dict = {}
             try:
                 if reqs:
                     info: dict = {}
                     results = f._run_batch(reqs, batch[0].max_mismatches, engine,
                                            stream.handle, info=info)
                     hits = info.get("hits")
+                    times = {k: info[k] for k in ("plan_s", "scan_s", "epilogue_s",
+                                                  "assemble_s") if k in info}
                     for r, res in zip(ready, results):
                         self._finish(r, res)
             except Exception as exc:
@@ -226,7 +252,7 @@ class SearchServer:
                     self.batches.append({"slot": slot, "requests": len(batch),
                                          "guides": sum(len(r.guides) for r in batch),
                                          "k": batch[0].max_mismatches, "hits": hits,
-                                         "seconds": time.perf_counter() - t0})
+                                         "seconds": time.perf_counter() - t0, **times})
 
     def _finish(self, r: Request, res) -> None:
         r.t_done = time.perf_counter()

@@ -621,6 +621,9 @@ def bench_serve(args, ws, rank, local):
     clocks = ClockSampler(local).start()
     srv = SearchServer(genome_data=genome, device=f"cuda:{local}", n_slots=args.slots,
                        memory_bytes=args.serve_memory << 30, max_batch_guides=args.batch_guides)
+    t_tune = time.perf_counter()
+    srv.warmup()
+    t_tune = time.perf_counter() - t_tune
     replay_server(srv, warm)
     b0 = len(srv.batches)
     x0 = [e.transfer() for e, _ in srv.slots]
@@ -634,8 +637,10 @@ def bench_serve(args, ws, rank, local):
         "requests_per_batch": float(np.mean([b["requests"] for b in batches])),
         "guides_per_batch": float(np.mean([b["guides"] for b in batches])),
         "slots": args.slots, "memory_gb": args.serve_memory,
-        "max_batch_guides": args.batch_guides,
-        "autotune": {str(k[0]): v.name for k, v in
+        "max_batch_guides": args.batch_guides, "tuning_warmup_s": t_tune,
+        "batch_seconds": {k: float(np.mean([b.get(k, 0.0) for b in batches]))
+                          for k in ("seconds", "plan_s", "scan_s", "epilogue_s", "assemble_s")},
+        "autotune": {f"k{k[0]}/size{k[1]}": v.name for k, v in
                      (srv.finder._tuner.cache.items() if srv.finder._tuner else [])}})
     srv.close()
     base = beguidedoff(None, max_mismatches=4, genome_data=genome, device=f"cuda:{local}",

@@ -53,3 +53,11 @@ def test_choose_picks_fastest_and_caches():
     ch2 = tuner.choose(plan2, ["NRN", "NGG"], 5)
     assert ch2 is ch and len(eng.calls) == n and plan2.tunings == [fast[2]]
     assert ch.as_dict()["tuning"]["split_families"] == fast[2][3]
+
+
+def test_coarse_signature_classes():
+    assert A.coarse_signature(1, 4) == (4, 0)
+    assert A.coarse_signature(16, 4) == (4, 0)
+    assert A.coarse_signature(17, 4) == (4, 1)
+    assert A.coarse_signature(300, 5) == (5, 3)
+    assert A.coarse_signature(5000, 3) == (3, 4)
