@@ -28,7 +28,7 @@ EXPORTED = [
     "bgo_scan_noalloc", "bgo_graph_create", "bgo_graph_launch", "bgo_graph_destroy",
     "bgo_epilogue_run", "bgo_synth_genome_repeats", "bgo_engine_transfer",
     "bgo_plan_set_tuning", "bgo_epilogue_fetch", "bgo_scan_time", "bgo_stream_create",
-    "bgo_stream_destroy",
+    "bgo_stream_destroy", "bgo_plan_families", "bgo_plan_set_family_tuning",
 ]
 
 INPUT_ROW_DTYPE = np.dtype([("plan_row", "<i4"), ("window_mask", "<u4"), ("target_base", "<i4"),
@@ -86,6 +86,8 @@ _SIGS = {
     "bgo_epilogue_fetch": ([_P, _P, _I64, _P], ctypes.c_int),
     "bgo_stream_create": ([ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "bgo_stream_destroy": ([_P], ctypes.c_int),
+    "bgo_plan_families": ([_P, _P], ctypes.c_int),
+    "bgo_plan_set_family_tuning": ([_P, _I32, _P], ctypes.c_int),
     "bgo_scan_time": ([_P, _P, _P, _P, _I32, _I32, _I32, _I32, _P,
                        ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "bgo_scan_noalloc": ([_P, _P, _I32, _P, _P, _P, _P, _I32, _I32, _P, _I64,
@@ -299,7 +301,9 @@ class Stream:
 class Tuning(ctypes.Structure):
     """bgo_tuning: launch parameters of scan modes 2 and 3 (0 = default)."""
     _fields_ = [("chunk_sites", ctypes.c_int32), ("group_guides", ctypes.c_int32),
-                ("ctas_per_sm", ctypes.c_int32), ("split_families", ctypes.c_int32)]
+                ("ctas_per_sm", ctypes.c_int32), ("split_families", ctypes.c_int32),
+                ("min_blocks", ctypes.c_int32), ("tolerance", ctypes.c_int32),
+                ("family_form", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Plan:
@@ -328,12 +332,30 @@ class Plan:
               "bgo_plan_info")
         return {"n_families": nf.value, "n_guides": ng.value}
 
-    def set_tuning(self, chunk_sites=0, group_guides=0, ctas_per_sm=0, split_families=0):
+    def set_tuning(self, chunk_sites=0, group_guides=0, ctas_per_sm=0, split_families=0,
+                   min_blocks=0, tolerance=0):
         """Launch parameters of scan modes 2 and 3 (see bgo_plan_set_tuning)."""
-        t = Tuning(int(chunk_sites), int(group_guides), int(ctas_per_sm), int(split_families))
+        t = Tuning(int(chunk_sites), int(group_guides), int(ctas_per_sm), int(split_families),
+                   int(min_blocks), int(tolerance))
         check(lib().bgo_plan_set_tuning(self.handle, ctypes.byref(t)), "bgo_plan_set_tuning")
         self.tuning = {"chunk_sites": int(chunk_sites), "group_guides": int(group_guides),
-                       "ctas_per_sm": int(ctas_per_sm), "split_families": int(split_families)}
+                       "ctas_per_sm": int(ctas_per_sm), "split_families": int(split_families),
+                       "min_blocks": int(min_blocks), "tolerance": int(tolerance)}
+
+    def set_family_tuning(self, family, chunk_sites=0, min_blocks=0, tolerance=0, form=0,
+                          ctas_per_sm=0):
+        """Launch parameters of one PAM family in split launches (form 0:
+        segment index, 1: every guide compared)."""
+        t = Tuning(int(chunk_sites), 0, int(ctas_per_sm), 1, int(min_blocks), int(tolerance),
+                   int(form))
+        check(lib().bgo_plan_set_family_tuning(self.handle, int(family), ctypes.byref(t)),
+              "bgo_plan_set_family_tuning")
+
+    def families(self):
+        """Family index of each plan row (-1: the row never matches)."""
+        out = np.empty(max(self.n_guides, 1), dtype=np.int32)
+        check(lib().bgo_plan_families(self.handle, out.ctypes.data), "bgo_plan_families")
+        return out[:self.n_guides]
 
     def close(self):
         if self.handle is not None and self.handle.value:

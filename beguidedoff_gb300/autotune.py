@@ -13,7 +13,11 @@ a power of two.
 
 Candidate parameters: scan mode; tile length (positions per warp chunk,
 ``chunk_sites``); guides per mask group (``group_guides``, mode 3); one
-launch per PAM family (``split_families``, mode 2).
+launch per PAM family (``split_families``, mode 2); CTAs per SM the kernel is
+compiled for (``min_blocks``: 3 with up to 80 registers, or 4 with up to 64,
+mode 2); mismatches tolerated per key region (``tolerance``: 0 with K + 1
+regions, or 1 with K / 2 + 1 regions and substitution-expanded buckets,
+mode 2).
 """
 from dataclasses import dataclass, field
 from typing import Dict, List, Sequence, Tuple
@@ -22,15 +26,33 @@ import numpy as np
 
 from . import _native
 
-# (name, mode, (chunk_sites, group_guides, ctas_per_sm, split_families))
-CANDIDATES: Tuple[Tuple[str, int, Tuple[int, int, int, int]], ...] = (
-    ("all-guides", 1, (0, 0, 0, 0)),
-    ("segment-index", 2, (0, 0, 0, 0)),
-    ("segment-index/per-family", 2, (0, 0, 0, 1)),
-    ("segment-masks/2048x128", 3, (2048, 128, 0, 0)),
-    ("segment-masks/1024x128", 3, (1024, 128, 0, 0)),
-    ("segment-masks/2048x64", 3, (2048, 64, 0, 0)),
+# (name, mode, (chunk_sites, group_guides, ctas_per_sm, split_families, min_blocks,
+#               tolerance))
+CANDIDATES: Tuple[Tuple[str, int, Tuple[int, int, int, int, int, int]], ...] = (
+    ("all-guides", 1, (0, 0, 0, 0, 0, 0)),
+    ("segment-index", 2, (0, 0, 0, 0, 0, 0)),
+    ("segment-index/1024/occ4", 2, (1024, 0, 0, 0, 4, 0)),
+    ("segment-index/per-family", 2, (0, 0, 0, 1, 0, 0)),
+    ("segment-index/per-family/1024/occ4", 2, (1024, 0, 0, 1, 4, 0)),
+    ("segment-index/t1", 2, (0, 0, 0, 0, 0, 1)),
+    ("segment-index/t1/1024", 2, (1024, 0, 0, 0, 0, 1)),
+    ("segment-index/t1/per-family", 2, (0, 0, 0, 1, 0, 1)),
+    ("segment-index/t1/per-family/1024", 2, (1024, 0, 0, 1, 0, 1)),
+    ("segment-masks/2048x128", 3, (2048, 128, 0, 0, 0, 0)),
 )
+TUNING_FIELDS = ("chunk_sites", "group_guides", "ctas_per_sm", "split_families", "min_blocks",
+                 "tolerance")
+# per PAM family, timed on a plan holding that family alone:
+# (name, form (0 segment index, 1 every guide), chunk_sites, min_blocks, tolerance)
+FAMILY_CANDIDATES = (
+    ("every-guide", 1, 0, 0, 0),
+    ("index", 0, 0, 0, 0),
+    ("index/1024/occ4", 0, 1024, 4, 0),
+    ("index/t1", 0, 0, 0, 1),
+    ("index/t1/1024", 0, 1024, 0, 1),
+    ("index/t1/1024/occ4", 0, 1024, 4, 1),
+)
+PER_FAMILY_TUNING = (0, 0, 0, 1, 0, 0)
 INDEXED_MAX_K = 7
 
 
@@ -38,16 +60,35 @@ INDEXED_MAX_K = 7
 class Choice:
     name: str
     mode: int
-    tuning: Tuple[int, int, int, int]
+    tuning: Tuple[int, int, int, int, int, int]
     times_ms: Dict[str, float] = field(default_factory=dict)
     sample_bp: int = 0
+    # per-family choice (name "per-family"): PAM -> (name, form, chunk_sites,
+    # min_blocks, tolerance, ms alone)
+    family: Dict[str, tuple] = field(default_factory=dict)
 
     def as_dict(self):
         return {"name": self.name, "mode": self.mode,
-                "tuning": dict(zip(("chunk_sites", "group_guides", "ctas_per_sm",
-                                    "split_families"), self.tuning)),
+                "tuning": dict(zip(TUNING_FIELDS, self.tuning)),
                 "times_ms": {k: round(v, 4) for k, v in self.times_ms.items()},
+                "family": {p: {"form": c[0], "ms": round(c[5], 4)} for p, c in
+                           self.family.items()},
                 "sample_bp": self.sample_bp}
+
+    def apply(self, plan, pams: Sequence[str]) -> None:
+        plan.set_tuning(*self.tuning)
+        if not self.family:
+            return
+        fam = plan.families()
+        done = set()
+        for row, f in enumerate(fam.tolist()):
+            if f < 0 or f in done:
+                continue
+            done.add(f)
+            c = self.family.get(pams[row].upper())
+            if c is not None:
+                plan.set_family_tuning(f, chunk_sites=c[2], min_blocks=c[3], tolerance=c[4],
+                                       form=c[1])
 
 
 def signature(pams: Sequence[str], max_mismatches: int) -> tuple:
@@ -129,9 +170,39 @@ class Autotuner:
                 if best is None or ms < best[0]:
                     best = (ms, name, mode, tune)
             hit = Choice(best[1], best[2], best[3], times, self.sample_bp)
+            if n_fam >= 2 and max_mismatches <= INDEXED_MAX_K and hasattr(plan, "guides"):
+                total, fam = self._per_family(plan, pams, max_mismatches, stream)
+                times["per-family"] = total
+                if total < best[0]:
+                    hit = Choice("per-family", 2, PER_FAMILY_TUNING, times, self.sample_bp, fam)
             self.cache[sig] = hit
-        plan.set_tuning(*hit.tuning)
+        hit.apply(plan, pams)
         return hit
+
+    def _per_family(self, plan, pams: Sequence[str], max_mismatches: int, stream=None):
+        """Each family timed alone in every family candidate; returns the sum
+        of the best times and the choice per family (keyed by PAM)."""
+        strands = self._sample()
+        ne = [0, 3][:len(strands)]
+        fam = plan.families()
+        total, out = 0.0, {}
+        for f in sorted(set(fam.tolist()) - {-1}):
+            rows = np.nonzero(fam == f)[0]
+            sub = _native.Plan(self.engine, plan.guides[rows], plan.pam_masks[rows],
+                               plan.pam_lens[rows], plan.pam_3prime[rows], stream)
+            try:
+                best = None
+                for name, form, chunk, minb, tol in FAMILY_CANDIDATES:
+                    sub.set_tuning(chunk, 0, 0, 0, minb, tol)
+                    ms = self.engine.scan_time(sub, strands, ne, max_mismatches,
+                                               1 if form == 1 else 2, self.reps, stream)
+                    if best is None or ms < best[5]:
+                        best = (name, form, chunk, minb, tol, ms)
+            finally:
+                sub.close()
+            out[pams[int(rows[0])].upper()] = best
+            total += best[5]
+        return total, out
 
     def close(self):
         for s in self._strands or []:

@@ -78,6 +78,7 @@ constexpr int kMaxKeyLen = 6;
 struct SeedSeg {
     uint8_t start, len, klen, pad;
     uint32_t off;  // first bucket offset of this segment in the offsets table
+    uint32_t ent;  // first entry of this segment's list, from the family's list_off
 };
 
 struct SeedFam {
@@ -202,8 +203,9 @@ struct bgo_plan {
     bgo::GuideRec *d_guides;
     bgo::FamilyDesc *h_fams;  // host copy (n_families)
     bgo::GuideRec *h_guides;  // host copy (n_active)
-    // segment index for one max_mismatches value, built on first use
+    // segment index for one (max_mismatches, tolerance) pair, built on first use
     int seed_k;               // -1000 = not built
+    std::vector<int> seed_tols;  // tolerance per family the index was built with
     int seed_ok;              // 0: the filter does not apply to this K
     unsigned char *d_seed;    // device block: families | offsets | lists
     bgo::SeedArgs seed;
@@ -216,14 +218,17 @@ struct bgo_plan {
     unsigned char *d_mask;    // device block: families | groups | table | guides
     bgo::MaskArgs mask;
     bgo_tuning tuning;        // launch parameters chosen by the caller (zeros = defaults)
+    std::vector<bgo_tuning> fam_tuning;  // per family (split launches); empty = tuning
 };
 
 namespace bgo {
 bool build_seed_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
+                      const std::vector<int> &tols,
                       std::vector<SeedFam> &out_fams, std::vector<uint32_t> &offsets,
                       std::vector<uint2> &entries, std::vector<uint16_t> &entry_idx);
-size_t seed_smem_bytes(const SeedArgs &sa);
-int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, cudaStream_t s);
+size_t seed_smem_bytes(const SeedArgs &sa, int chunk_sites);
+int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
+                       int min_blocks, int tolerance, int ctas_per_sm, cudaStream_t s);
 void pam_program(const FamilyDesc &F, SeedFam &sf);
 bool build_mask_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
                       int group_max, std::vector<MaskFam> &out_fams,

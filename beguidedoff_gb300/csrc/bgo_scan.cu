@@ -397,17 +397,48 @@ extern "C" int bgo_plan_destroy(bgo_plan *pl) {
     return BGO_OK;
 }
 
-extern "C" int bgo_plan_set_tuning(bgo_plan *pl, const bgo_tuning *t) {
+static int check_tuning(const bgo_plan *pl, const bgo_tuning *t) {
     if (!pl || !t) return BGO_ERR_ARG;
     if ((t->chunk_sites != 0 && t->chunk_sites != 1024 && t->chunk_sites != 2048) ||
         (t->group_guides != 0 && t->group_guides != 32 && t->group_guides != 64 &&
          t->group_guides != 128) ||
-        t->ctas_per_sm < 0 || t->split_families < 0 || t->split_families > 1) {
+        t->ctas_per_sm < 0 || t->split_families < 0 || t->split_families > 1 ||
+        (t->min_blocks != 0 && t->min_blocks != 3 && t->min_blocks != 4) || t->tolerance < 0 ||
+        t->tolerance > 1 || t->family_form < 0 || t->family_form > 1) {
         set_error("bgo_plan_set_tuning: chunk_sites 1024|2048, group_guides 32|64|128, "
-                  "ctas_per_sm >= 0, split_families 0|1");
+                  "ctas_per_sm >= 0, split_families 0|1, min_blocks 3|4, tolerance 0|1, "
+                  "family_form 0|1");
         return BGO_ERR_ARG;
     }
+    return BGO_OK;
+}
+
+extern "C" int bgo_plan_set_tuning(bgo_plan *pl, const bgo_tuning *t) {
+    const int rc = check_tuning(pl, t);
+    if (rc != BGO_OK) return rc;
     pl->tuning = *t;
+    pl->fam_tuning.clear();
+    return BGO_OK;
+}
+
+extern "C" int bgo_plan_set_family_tuning(bgo_plan *pl, int32_t family, const bgo_tuning *t) {
+    const int rc = check_tuning(pl, t);
+    if (rc != BGO_OK) return rc;
+    if (family < 0 || family >= pl->n_families) {
+        set_error("bgo_plan_set_family_tuning: no such family");
+        return BGO_ERR_ARG;
+    }
+    if (pl->fam_tuning.empty()) pl->fam_tuning.assign((size_t)pl->n_families, pl->tuning);
+    pl->fam_tuning[(size_t)family] = *t;
+    return BGO_OK;
+}
+
+extern "C" int bgo_plan_families(const bgo_plan *pl, int32_t *row_family) {
+    if (!pl || (pl->n_guides > 0 && !row_family)) return BGO_ERR_ARG;
+    for (int32_t i = 0; i < pl->n_guides; ++i) row_family[i] = -1;
+    for (int f = 0; f < pl->n_families; ++f)
+        for (int g = pl->h_fams[f].gbeg; g < pl->h_fams[f].gend; ++g)
+            row_family[pl->h_guides[g].row] = f;
     return BGO_OK;
 }
 
@@ -433,11 +464,37 @@ static void fill_strand(StrandDesc &d, const bgo_genome *g, int32_t n_encoded, i
     d.pad = 0;
 }
 
-// Builds (once per max_mismatches value) and uploads the plan's segment
-// index.  Returns 1 when the index applies, 0 when the scan must compare every
-// guide (mode 1), or a negative BGO_ERR_*.
+// Builds (once per (max_mismatches, tolerance)) and uploads the plan's segment
+// index and its per-family views.  Returns 1 when the index applies to the
+// plan's launch form (all families in one launch, or one launch per family),
+// 0 when the scan must compare every guide (mode 1), or a negative BGO_ERR_*.
+static const bgo_tuning &family_tuning(const bgo_plan *pl, int f) {
+    return pl->fam_tuning.empty() ? pl->tuning : pl->fam_tuning[(size_t)f];
+}
+
 static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s) {
-    if (pl->seed_k == K) return pl->seed_ok;
+    const bool split = pl->tuning.split_families && pl->n_families > 1;
+    std::vector<int> tols((size_t)pl->n_families, pl->tuning.tolerance);
+    if (split)
+        for (int f = 0; f < pl->n_families; ++f) tols[(size_t)f] = family_tuning(pl, f).tolerance;
+    const size_t limit = 220 * 1024;
+    auto chunk_of = [](const bgo_tuning &t) { return t.chunk_sites ? t.chunk_sites : 2048; };
+    auto applies = [&]() -> int {
+        if (!pl->seed_ok) return 0;
+        if (split) {
+            for (int f = 0; f < pl->n_families; ++f) {
+                const bgo_tuning &t = family_tuning(pl, f);
+                if (t.family_form == 0 &&
+                    seed_smem_bytes(pl->seed_fam[(size_t)f], chunk_of(t)) > limit)
+                    return 0;
+            }
+            return 1;
+        }
+        for (int v : tols)
+            if (v != tols[0]) return 0;  // one launch needs one tolerance
+        return seed_smem_bytes(pl->seed, chunk_of(pl->tuning)) <= limit ? 1 : 0;
+    };
+    if (pl->seed_k == K && pl->seed_tols == tols) return applies();
     if (pl->d_seed || pl->d_seed_fam) {
         BGO_CUDA(cudaStreamSynchronize(s));
         if (pl->d_seed) cudaFree(pl->d_seed);
@@ -447,12 +504,13 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
     }
     pl->seed_fam.clear();
     pl->seed_k = K;
+    pl->seed_tols = tols;
     pl->seed_ok = 0;
     std::vector<SeedFam> sf;
     std::vector<uint32_t> offs;
     std::vector<uint2> ents;
     std::vector<uint16_t> eidx;
-    if (!build_seed_index(pl->h_fams, pl->n_families, pl->h_guides, K, sf, offs, ents, eidx))
+    if (!build_seed_index(pl->h_fams, pl->n_families, pl->h_guides, K, tols, sf, offs, ents, eidx))
         return 0;
     const size_t b_f = sizeof(SeedFam) * sf.size();
     const size_t b_e = sizeof(uint2) * ents.size();
@@ -465,8 +523,6 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
     sa.n_guides = pl->n_active;
     sa.n_offsets = (int32_t)offs.size();
     sa.n_lists = (int32_t)ents.size();
-    // the whole index must fit in shared memory beside the warps' chunk slices
-    if (seed_smem_bytes(sa) > 200 * 1024) return 0;
     BGO_CUDA(cudaMalloc(&pl->d_seed, o_i + b_i + 16));
     BGO_CUDA(cudaMemcpyAsync(pl->d_seed, sf.data(), b_f, cudaMemcpyHostToDevice, s));
     if (b_e) {
@@ -486,18 +542,16 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
     std::vector<SeedFam> rebased(sf);
     std::vector<SeedArgs> views(sf.size());
     for (size_t f = 0; f < sf.size(); ++f) {
-        const FamilyDesc &F = pl->h_fams[f];
-        const uint32_t G = (uint32_t)(F.gend - F.gbeg);
         const uint32_t off0 = sf[f].seg[0].off;
-        const uint32_t off_end =
-            f + 1 < sf.size() ? sf[f + 1].seg[0].off : (uint32_t)offs.size();
+        const uint32_t off_end = f + 1 < sf.size() ? sf[f + 1].seg[0].off : (uint32_t)offs.size();
+        const uint32_t list_end = f + 1 < sf.size() ? sf[f + 1].list_off : (uint32_t)ents.size();
         rebased[f].list_off = 0;
         for (int j = 0; j < sf[f].nseg; ++j) rebased[f].seg[j].off = sf[f].seg[j].off - off0;
         SeedArgs v{};
         v.n_fams = 1;
-        v.n_guides = (int32_t)G;
+        v.n_guides = pl->h_fams[f].gend - pl->h_fams[f].gbeg;
         v.n_offsets = (int32_t)(off_end - off0);
-        v.n_lists = (int32_t)((uint32_t)sf[f].nseg * G);
+        v.n_lists = (int32_t)(list_end - sf[f].list_off);
         v.entries = sa.entries + sf[f].list_off;
         v.entry_idx = sa.entry_idx + sf[f].list_off;
         v.offsets = sa.offsets + off0;
@@ -512,7 +566,7 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
         views[f].fams = reinterpret_cast<const SeedFam *>(pl->d_seed_fam) + f;
     pl->seed_fam = views;
     pl->seed_ok = 1;
-    return 1;
+    return applies();
 }
 
 // Builds (once per (max_mismatches, group size)) and uploads the plan's
@@ -640,27 +694,50 @@ extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
         if (rc != BGO_OK) return rc;
         engine->launches++;
     } else if (seeded == 1) {
-        for (int i = 0; i < n_strands; ++i) {
-            fill_strand(p.strand[i], strands[i], n_encoded[i], i);
-            p.strand[i].n_tiles = seed_tiles_for(strands[i]->total_bp);
-        }
-        p.n_strands = n_strands;
-        p.tiles_total = p.strand[0].n_tiles + (n_strands > 1 ? p.strand[1].n_tiles : 0);
-        if (p.tiles_total == 0) return BGO_OK;
+        // one launch over all families, or one per family with its own form
+        auto seed_launch = [&](int fb, int fe, const SeedArgs &sa, const bgo_tuning &t) -> int {
+            const int chunk = t.chunk_sites ? t.chunk_sites : 2048;
+            const int minb = t.min_blocks ? t.min_blocks : 3;
+            ScanParams q = p;
+            for (int i = 0; i < n_strands; ++i) {
+                fill_strand(q.strand[i], strands[i], n_encoded[i], i);
+                q.strand[i].n_tiles = seed_tiles_for(strands[i]->total_bp, chunk);
+            }
+            q.n_strands = n_strands;
+            q.tiles_total = q.strand[0].n_tiles + (n_strands > 1 ? q.strand[1].n_tiles : 0);
+            if (q.tiles_total == 0) return BGO_OK;
+            q.fam_begin = fb;
+            q.fam_end = fe;
+            const int rc = launch_seed_kernel(q, sa, engine->sm_count, chunk, minb, t.tolerance,
+                                              t.ctas_per_sm, s);
+            if (rc == BGO_OK) engine->launches++;
+            return rc;
+        };
+        auto every_guide_launch = [&](int fb, int fe) -> int {
+            ScanParams q = p;
+            for (int i = 0; i < n_strands; ++i) fill_strand(q.strand[i], strands[i], n_encoded[i], i);
+            q.n_strands = n_strands;
+            q.tiles_total = q.strand[0].n_tiles + (n_strands > 1 ? q.strand[1].n_tiles : 0);
+            if (q.tiles_total == 0) return BGO_OK;
+            q.fam_begin = fb;
+            q.fam_end = fe;
+            const int64_t grid = std::min<int64_t>(q.tiles_total, max_grid);
+            scan_kernel<<<(unsigned)grid, kTileThreads, 0, s>>>(q);
+            BGO_CUDA(cudaGetLastError());
+            engine->launches++;
+            return BGO_OK;
+        };
         if (plan->tuning.split_families && plan->n_families > 1) {
             for (int f = 0; f < plan->n_families; ++f) {
-                p.fam_begin = f;
-                p.fam_end = f + 1;
-                const int rc = launch_seed_kernel(p, plan->seed_fam[(size_t)f], engine->sm_count, s);
+                const bgo_tuning &t = family_tuning(plan, f);
+                const int rc = t.family_form == 1
+                                   ? every_guide_launch(f, f + 1)
+                                   : seed_launch(f, f + 1, plan->seed_fam[(size_t)f], t);
                 if (rc != BGO_OK) return rc;
-                engine->launches++;
             }
         } else {
-            p.fam_begin = 0;
-            p.fam_end = plan->n_families;
-            const int rc = launch_seed_kernel(p, plan->seed, engine->sm_count, s);
+            const int rc = seed_launch(0, plan->n_families, plan->seed, plan->tuning);
             if (rc != BGO_OK) return rc;
-            engine->launches++;
         }
     } else {
         for (int i = 0; i < n_strands; ++i) fill_strand(p.strand[i], strands[i], n_encoded[i], i);

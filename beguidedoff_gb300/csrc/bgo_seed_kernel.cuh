@@ -1,0 +1,362 @@
+// Segment-indexed scan kernel (scan mode 2), included by the translation
+// units that instantiate it for tolerance 0 (bgo_seed.cu) and tolerance 1
+// (bgo_seed_t1.cu), which compile in parallel.  The algorithm is described at
+// the top of bgo_seed.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "bgo_device.cuh"
+#include "bgo_internal.cuh"
+
+namespace bgo {
+
+
+constexpr int kSeedWarps = kSeedThreads / 32;
+constexpr int kQueueCap = 32 * (kSeedMaxK + 1);  // bucket ranges per round
+
+// Per-warp shared-memory slice for chunks of CH positions: two chunk buffers
+// (H, L, N planes), the compacted list, the round's position records and the
+// bucket-range queue (word + count).
+template <int CH>
+struct SeedChunk {
+    static constexpr int kRows = CH / 1024;      // 32-position words per lane
+    static constexpr int kWords = CH / 32 + 4;   // + halo, a multiple of 4 words
+    static constexpr int kVecs = kWords / 4;     // 16-byte copies per plane
+    static constexpr size_t kBuf = 3 * kWords * sizeof(uint32_t);
+    static constexpr size_t kListOff = 2 * kBuf;
+    static constexpr size_t kRecOff = (kListOff + CH * sizeof(uint16_t) + 15) / 16 * 16;
+    static constexpr size_t kQueueOff = kRecOff + 32 * sizeof(uint4);
+    static constexpr size_t kCountOff = kQueueOff + kQueueCap * sizeof(uint32_t);
+    static constexpr size_t kSlice = (kCountOff + kQueueCap * sizeof(uint16_t) + 15) / 16 * 16;
+    static_assert(kWords % 4 == 0, "chunk copies are whole 16-byte vectors");
+    static_assert(kBuf % 16 == 0, "chunk buffers stay 16-byte aligned");
+};
+
+// The key regions for K mismatches and tolerance TOL: S = K / (TOL + 1) + 1
+// disjoint segments over the 20 guide positions, keyed by their first <= 6
+// bases.  S * (TOL + 1) > K, so every hit has a region with <= TOL mismatches.
+template <int K, int TOL>
+struct SegT {
+    static constexpr int S = K / (TOL + 1) + 1;
+    static constexpr int q = kGuideLen / S, r = kGuideLen % S;
+    __host__ __device__ static constexpr int start(int j) { return j * q + (j < r ? j : r); }
+    __host__ __device__ static constexpr int len(int j) { return q + (j < r ? 1 : 0); }
+    __host__ __device__ static constexpr int klen(int j) {
+        return len(j) < kMaxKeyLen ? len(j) : kMaxKeyLen;
+    }
+};
+
+// The full check of a candidate whose raw count cm <= K, found through
+// region j: emits the hit if j is its first region with <= TOL mismatches
+// and it stays within K after the N correction.
+template <int K, int TOL>
+__device__ __noinline__ void finish_candidate(const ScanParams &p, uint32_t m, int cm, uint2 e,
+                                              uint32_t idx, int j, uint32_t n20g, uint32_t ne,
+                                              uint64_t slot, uint64_t pos, uint32_t gbeg) {
+    using G = SegT<K, TOL>;
+    bool first = true;
+#pragma unroll
+    for (int jj = 0; jj < G::S - 1; ++jj)
+        if (jj < j)
+            first = first && __popc((m >> G::start(jj)) & ((1u << G::klen(jj)) - 1u)) > TOL;
+    if (!first) return;
+    int mmf = cm;
+    if (n20g) {
+        const uint32_t eh = (ne & 2u) ? e.x : ~e.x;
+        const uint32_t el = (ne & 1u) ? e.y : ~e.y;
+        mmf = cm + __popc(n20g & eh & el);
+    }
+    if (mmf > K) return;
+    const uint32_t row = __ldg(&p.guides[gbeg + idx].row);
+    semit(((uint64_t)row << 39) | (slot << 38) | (pos << 6) | (uint64_t)mmf, p.keys, p.cap,
+          p.counter);
+}
+
+template <int K, int TOL, int CH, int MINB>
+__global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParams p, SeedArgs sa) {
+    using G = SegT<K, TOL>;
+    constexpr int S = G::S;
+    using C = SeedChunk<CH>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    SeedFam *sFam = reinterpret_cast<SeedFam *>(smem);
+    uint2 *sEnt = reinterpret_cast<uint2 *>(sFam + sa.n_fams);
+    uint32_t *sOff = reinterpret_cast<uint32_t *>(sEnt + sa.n_lists);
+    uint16_t *sIdx = reinterpret_cast<uint16_t *>(sOff + sa.n_offsets);
+    unsigned char *slices =
+        smem + ((sizeof(SeedFam) * sa.n_fams + sizeof(uint2) * sa.n_lists +
+                 sizeof(uint32_t) * sa.n_offsets + sizeof(uint16_t) * sa.n_lists + 15) / 16 * 16);
+    __shared__ unsigned long long sCand;
+
+    const int t = threadIdx.x;
+    const int lane = t & 31;
+    const int warp = t >> 5;
+    unsigned char *slice = slices + warp * C::kSlice;
+    uint16_t *wList = reinterpret_cast<uint16_t *>(slice + C::kListOff);
+    uint4 *wRec = reinterpret_cast<uint4 *>(slice + C::kRecOff);
+    uint32_t *wQ = reinterpret_cast<uint32_t *>(slice + C::kQueueOff);
+    uint16_t *wCnt = reinterpret_cast<uint16_t *>(slice + C::kCountOff);
+
+    for (int i = t; i < sa.n_fams; i += kSeedThreads) sFam[i] = sa.fams[i];
+    for (int i = t; i < sa.n_lists; i += kSeedThreads) {
+        sEnt[i] = sa.entries[i];
+        sIdx[i] = sa.entry_idx[i];
+    }
+    for (int i = t; i < sa.n_offsets; i += kSeedThreads) sOff[i] = sa.offsets[i];
+    if (t == 0) sCand = 0;
+    __syncthreads();
+
+    const int64_t chunks0 = p.strand[0].n_tiles;
+    const int64_t n_chunks = p.tiles_total;
+    const int64_t stride = (int64_t)gridDim.x * kSeedWarps;
+    // Chunk c's words [c*CH/32, c*CH/32 + kWords) of the three planes, copied
+    // into buffer b as 16-byte vectors (the planes are padded so that the copy
+    // never leaves them, and zero beyond total_bp).
+    auto issue = [&](int64_t c, int b) {
+        const bool second = c >= chunks0;
+        const int64_t w0 = (second ? c - chunks0 : c) * (CH / 32);
+        const StrandDesc &sd = second ? p.strand[1] : p.strand[0];
+        uint32_t *dst = reinterpret_cast<uint32_t *>(slice + b * C::kBuf);
+        for (int i = lane; i < 3 * C::kVecs; i += 32) {
+            const int plane = i / C::kVecs, v = i - plane * C::kVecs;
+            const uint32_t *src = plane == 0 ? sd.H : plane == 1 ? sd.L : sd.N;
+            cp_async16(dst + plane * C::kWords + 4 * v, src + w0 + 4 * v);
+        }
+    };
+    uint32_t cand = 0;
+    const int64_t c_first = (int64_t)blockIdx.x * kSeedWarps + warp;
+    if (c_first < n_chunks) issue(c_first, 0);
+    cp_async_commit();
+    int buf = 0;
+    for (int64_t c = c_first; c < n_chunks; c += stride, buf ^= 1) {
+        if (c + stride < n_chunks) issue(c + stride, buf ^ 1);
+        cp_async_commit();
+        cp_async_wait<1>();  // this chunk's copies are done; the next one is in flight
+        __syncwarp();
+        const uint32_t *wH = reinterpret_cast<const uint32_t *>(slice + buf * C::kBuf);
+        const uint32_t *wL = wH + C::kWords;
+        const uint32_t *wN = wL + C::kWords;
+        const bool second = c >= chunks0;
+        const int64_t lc = second ? c - chunks0 : c;
+        const int64_t total_bp = second ? p.strand[1].total_bp : p.strand[0].total_bp;
+        const int has_n = second ? p.strand[1].has_n : p.strand[0].has_n;
+        const uint32_t ne = (uint32_t)(second ? p.strand[1].n_encoded : p.strand[0].n_encoded);
+        const uint64_t slot = (uint64_t)(second ? p.strand[1].slot : p.strand[0].slot);
+        const int64_t base = lc * CH;
+        // positions [0, lim) of this chunk are scanned (total_bp - 26 overall)
+        const int64_t lim64 = total_bp - kSiteSpan - base;
+        const int lim = lim64 > CH ? CH : (int)lim64;
+
+        for (int f = p.fam_begin; f < p.fam_end; ++f) {
+            const FamilyDesc F = p.fams[f];
+            const uint32_t win_off = F.three_prime ? 0u : (uint32_t)F.plen;
+            const int n_tests = sFam[f - p.fam_begin].n_tests;
+            uint32_t tsh[kMaxPam], tcd[kMaxPam];
+#pragma unroll
+            for (int k = 0; k < kMaxPam; ++k) {
+                tsh[k] = sFam[f - p.fam_begin].pam_shift[k];
+                tcd[k] = sFam[f - p.fam_begin].pam_code[k];
+            }
+            uint32_t pass[C::kRows];
+            int cnt = 0;
+#pragma unroll
+            for (int u = 0; u < C::kRows; ++u) {
+                const int wi = u * 32 + lane;
+                const int rem = lim - 32 * wi;
+                uint32_t ps = rem >= 32 ? 0xFFFFFFFFu : (rem <= 0 ? 0u : (1u << rem) - 1u);
+                const uint32_t h0 = wH[wi], h1 = wH[wi + 1], l0 = wL[wi], l1 = wL[wi + 1];
+#pragma unroll
+                for (int k = 0; k < kMaxPam; ++k) {
+                    if (k < n_tests)
+                        ps &= pam_test(sfshr(h0, h1, tsh[k]), sfshr(l0, l1, tsh[k]), tcd[k]);
+                }
+                pass[u] = ps;
+                cnt += __popc(ps);
+            }
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            int off = incl - cnt;
+#pragma unroll
+            for (int u = 0; u < C::kRows; ++u) {
+                uint32_t m = pass[u];
+                while (m) {
+                    const int j = __ffs(m) - 1;
+                    m &= m - 1u;
+                    wList[off++] = (uint16_t)(32 * (u * 32 + lane) + j);
+                }
+            }
+            __syncwarp();
+            // the family's bucket tables and entry bases, held in registers
+            uint32_t seg_off[S], seg_ent[S];
+            {
+                const uint32_t list_off = sFam[f - p.fam_begin].list_off;
+#pragma unroll
+                for (int j = 0; j < S; ++j) {
+                    seg_off[j] = sFam[f - p.fam_begin].seg[j].off;
+                    seg_ent[j] = list_off + sFam[f - p.fam_begin].seg[j].ent;
+                }
+            }
+            const uint32_t gbeg = (uint32_t)F.gbeg;
+            for (int k0 = 0; k0 < total; k0 += 32) {
+                const int k = k0 + lane;
+                const bool has = k < total;
+                uint32_t s = 0, h20 = 0, l20 = 0, n20g = 0;
+                if (has) {
+                    s = wList[k];
+                    const uint32_t wo = s + win_off;
+                    const uint32_t wi = wo >> 5, b = wo & 31u;
+                    h20 = sfshr(wH[wi], wH[wi + 1], b) & 0xFFFFFu;
+                    l20 = sfshr(wL[wi], wL[wi + 1], b) & 0xFFFFFu;
+                    if (has_n) {
+                        const uint32_t n26 =
+                            sfshr(wN[s >> 5], wN[(s >> 5) + 1], s & 31u) & 0x3FFFFFFu;
+                        if (n26) n20g = sfshr(wN[wi], wN[wi + 1], b) & 0xFFFFFu;
+                    }
+                }
+                const uint64_t pos = (uint64_t)(base + s);
+                // Branch-free in three phases so that the regions' load
+                // chains overlap: (1) every region's bucket descriptor, (2) an
+                // inline compare of every bucket's first guide (an empty
+                // bucket compares its region list's first entry, always
+                // present, and ignores the result), (3) the rare candidates
+                // within K.  Further guides of a bucket stay as a range.
+                uint32_t rn[S], e0v[S];
+                uint32_t T = 0, R = 0, within = 0;
+#pragma unroll
+                for (int j = 0; j < S; ++j) {
+                    const int st = G::start(j), kl = G::klen(j);
+                    const uint32_t km = (1u << kl) - 1u;
+                    const uint32_t code = (((h20 >> st) & km) << kl) | ((l20 >> st) & km);
+                    const uint32_t d = has ? sOff[seg_off[j] + code] : 0u;
+                    const uint32_t n = d >> 16;
+                    e0v[j] = seg_ent[j] + (d & 0xFFFFu);
+                    T += n;
+                    rn[j] = n > 1u ? n - 1u : 0u;
+                    R += rn[j] != 0u;
+                    if (n == 0u) e0v[j] = seg_ent[j];
+                    within |= (n != 0u ? 1u : 0u) << j;
+                }
+#pragma unroll
+                for (int j = 0; j < S; ++j) {
+                    const uint2 e = sEnt[e0v[j]];
+                    if (__popc((h20 ^ e.x) | (l20 ^ e.y)) > K) within &= ~(1u << j);
+                }
+                if (within) {
+#pragma unroll
+                    for (int j = 0; j < S; ++j) {
+                        if (within & (1u << j)) {
+                            const uint2 e = sEnt[e0v[j]];
+                            const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
+                            finish_candidate<K, TOL>(p, m, __popc(m), e, sIdx[e0v[j]], j, n20g,
+                                                     ne, slot, pos, gbeg);
+                        }
+                    }
+                }
+                cand += T;
+                // buckets with more than one guide: ranges through the queue
+                if (!__any_sync(0xFFFFFFFFu, R != 0u)) continue;
+                uint32_t rin = R;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, rin, o);
+                    if (lane >= o) rin += v;
+                }
+                const uint32_t RT = __shfl_sync(0xFFFFFFFFu, rin, 31);
+                wRec[lane] = make_uint4(h20, l20, n20g, s);
+                uint32_t qp = rin - R;
+#pragma unroll
+                for (int j = 0; j < S; ++j) {
+                    if (rn[j]) {
+                        wQ[qp] = (e0v[j] + 1u) | ((uint32_t)j << 22) | ((uint32_t)lane << 27);
+                        wCnt[qp] = (uint16_t)rn[j];
+                        ++qp;
+                    }
+                }
+                __syncwarp();
+                for (uint32_t q = lane; q < RT; q += 32) {
+                    const uint32_t v = wQ[q];
+                    const uint32_t n = wCnt[q];
+                    const uint4 r = wRec[v >> 27];
+                    const uint32_t e0 = v & 0x3FFFFFu;
+                    const int j = (int)((v >> 22) & 31u);
+                    for (uint32_t i = 0; i < n; ++i) {
+                        const uint2 e = sEnt[e0 + i];
+                        const uint32_t m = (r.x ^ e.x) | (r.y ^ e.y);
+                        const int cm = __popc(m);
+                        if (cm <= K)
+                            finish_candidate<K, TOL>(p, m, cm, e, sIdx[e0 + i], j, r.z, ne, slot,
+                                                (uint64_t)(base + r.w), gbeg);
+                    }
+                }
+                __syncwarp();
+            }
+            __syncwarp();
+        }
+    }
+    cp_async_wait<0>();
+    for (int o = 16; o > 0; o >>= 1) cand += __shfl_down_sync(0xFFFFFFFFu, cand, o);
+    if (lane == 0 && cand) atomicAdd(&sCand, (unsigned long long)cand);
+    __syncthreads();
+    if (t == 0 && sCand) atomicAdd(p.counter + 1, sCand);
+}
+
+template <int K, int TOL, int CH, int MINB>
+static int launch_k(const ScanParams &p, const SeedArgs &sa, int sm_count, int ctas_per_sm,
+                    cudaStream_t s) {
+    const size_t smem = seed_smem_bytes(sa, CH);
+    static size_t configured = 0;
+    if (smem > configured) {
+        BGO_CUDA(cudaFuncSetAttribute(scan_seed_kernel<K, TOL, CH, MINB>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    int per_sm = 0;
+    BGO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, scan_seed_kernel<K, TOL, CH, MINB>, kSeedThreads, smem));
+    if (per_sm < 1) per_sm = 1;
+    if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
+    const int64_t blocks_needed = (p.tiles_total + kSeedWarps - 1) / kSeedWarps;
+    const int64_t grid = std::min<int64_t>(blocks_needed, (int64_t)sm_count * per_sm);
+    scan_seed_kernel<K, TOL, CH, MINB><<<(unsigned)grid, kSeedThreads, smem, s>>>(p, sa);
+    BGO_CUDA(cudaGetLastError());
+    return BGO_OK;
+}
+
+template <int TOL, int CH, int MINB>
+static int launch_cm(const ScanParams &p, const SeedArgs &sa, int sm_count, int ctas_per_sm,
+                     cudaStream_t s) {
+    switch (p.max_mm) {
+        case 0: return launch_k<0, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 1: return launch_k<1, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 2: return launch_k<2, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 3: return launch_k<3, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 4: return launch_k<4, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 5: return launch_k<5, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 6: return launch_k<6, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 7: return launch_k<7, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        default:
+            set_error("segment index: max_mismatches outside 0..7");
+            return BGO_ERR_ARG;
+    }
+}
+
+// All chunk lengths and occupancy targets for one tolerance.
+template <int TOL>
+static int launch_tol(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
+                      int min_blocks, int ctas_per_sm, cudaStream_t s) {
+    const bool c1k = chunk_sites == 1024;
+    if (min_blocks == 4)
+        return c1k ? launch_cm<TOL, 1024, 4>(p, sa, sm_count, ctas_per_sm, s)
+                   : launch_cm<TOL, 2048, 4>(p, sa, sm_count, ctas_per_sm, s);
+    return c1k ? launch_cm<TOL, 1024, 3>(p, sa, sm_count, ctas_per_sm, s)
+               : launch_cm<TOL, 2048, 3>(p, sa, sm_count, ctas_per_sm, s);
+}
+
+}  // namespace bgo

@@ -161,13 +161,23 @@ _IUPAC = {"A": "A", "C": "C", "G": "G", "T": "T", "R": "AG", "Y": "CT", "S": "CG
 
 def guide_pams(args, n):
     """PAM of each guide: all NGG (plain configuration) or the mixed-family
-    split of the batched and hit-dense configurations."""
+    split of the batched and hit-dense configurations (restricted to
+    ``--families`` when given: the same guides, only those families)."""
     if args.config == "plain":
         return ["NGG"] * n
     pams = []
     for pam, frac in MIXED_FAMILIES:
         pams += [pam] * int(round(frac * n))
     return (pams + ["NGG"] * n)[:n]
+
+
+def select_families(args, guides, pams):
+    keep = getattr(args, "families", None)
+    if not keep:
+        return guides, pams
+    keep = {p.strip().upper() for p in keep.split(",")}
+    idx = [i for i, p in enumerate(pams) if p in keep]
+    return [guides[i] for i in idx], [pams[i] for i in idx]
 
 
 def dense_guides(families, pams, seed=3):
@@ -242,6 +252,8 @@ def bench_reference(args, ws, rank):
                                   repeats=DENSE_REPEATS if args.config == "dense" else None)
     if args.config == "dense":
         guides = dense_guides(genome["repeat_families"], pams)
+    guides, pams = select_families(args, guides, pams)
+    args.guides = len(guides)
     from beguidedoff_gb300.finder import prepare_n_masks
 
     genome["_nm_fwd_le"], genome["_nm_rc_le"] = prepare_n_masks(genome)
@@ -328,6 +340,8 @@ def bench_ours(args, ws, rank, local):
     pams = guide_pams(args, len(guides))
     if dense:
         guides = dense_guides(genome["repeat_families"], pams)
+    guides, pams = select_families(args, guides, pams)
+    args.guides = len(guides)
     t0 = time.perf_counter()
     f = beguidedoff(None, max_mismatches=args.max_mm, genome_data=genome,
                     device=f"cuda:{local}", scan_mode=args.mode)
@@ -698,6 +712,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--families", default="", help="mixed/dense: keep only these PAM families "
+                                                   "(comma list), e.g. NRN")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: requests per second")
     ap.add_argument("--duration", type=float, default=15.0, help="serve: trace seconds")
     ap.add_argument("--slots", type=int, default=2, help="serve: concurrent batches")

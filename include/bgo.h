@@ -136,7 +136,7 @@ int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
 /*
  * Launch parameters of a plan (scan modes 2 and 3), normally chosen by the
  * autotuner (beguidedoff_gb300/autotune.py).  Zero fields keep the defaults.
- *   chunk_sites   positions per warp chunk ("tile length"): 1024 or 2048
+ *   chunk_sites   modes 2/3: positions per warp chunk ("tile length"): 1024 or 2048
  *   group_guides  mode 3: guides per mask group ("guides per block"): 32, 64
  *                 or 128; a family larger than this is cut into several groups
  *   ctas_per_sm   cap on resident CTAs per SM for the grid size (0 = the
@@ -144,6 +144,11 @@ int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
  *   split_families  mode 2: one launch per PAM family, each holding only its
  *                 family's index in shared memory (higher occupancy when the
  *                 combined index is large), instead of one launch for all
+ *   min_blocks    mode 2: CTAs per SM the kernel is compiled for, 3 (up to 80
+ *                 registers per thread) or 4 (up to 64); 0 = 3
+ *   tolerance     mode 2: mismatches allowed in a key region, 0 (K + 1 exact
+ *                 regions) or 1 (K / 2 + 1 regions, guides also indexed under
+ *                 every single-base substitution of their keys)
  * Changing group_guides rebuilds the mask index at the next launch.  No
  * reference counterpart: the reference fixes 256 threads x 200 Mbp chunks.
  */
@@ -152,8 +157,23 @@ typedef struct bgo_tuning {
     int32_t group_guides;
     int32_t ctas_per_sm;
     int32_t split_families;
+    int32_t min_blocks;
+    int32_t tolerance;
+    int32_t family_form;   /* per-family tuning only: 0 segment index, 1 compare every guide */
+    int32_t reserved;
 } bgo_tuning;
 int bgo_plan_set_tuning(bgo_plan *plan, const bgo_tuning *tuning);
+
+/*
+ * Per-family launch parameters for scan mode 2 with split_families: family f
+ * gets its own form (segment index, or every guide compared as in mode 1),
+ * tolerance, chunk_sites, min_blocks and ctas_per_sm.  Families are numbered
+ * in first-seen order of their PAM pattern; bgo_plan_families writes each
+ * plan row's family (-1 for rows that never match).  Families without their
+ * own setting use the plan's.
+ */
+int bgo_plan_families(const bgo_plan *plan, int32_t *row_family);
+int bgo_plan_set_family_tuning(bgo_plan *plan, int32_t family, const bgo_tuning *tuning);
 
 /*
  * Times the scan: one untimed launch, then `reps` launches each bracketed by

@@ -10,6 +10,10 @@ class FakePlan:
     def set_tuning(self, *t):
         self.tunings.append(tuple(t))
 
+    def families(self):
+        import numpy as np
+        return np.zeros(0, dtype=np.int32)
+
 
 class FakeEngine:
     def __init__(self, times):

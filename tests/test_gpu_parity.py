@@ -25,7 +25,7 @@ def _lib():
 
 
 @pytest.mark.parametrize("mode,epilogue", [(0, "device"), (1, "device"), (2, "device"),
-                                           (3, "device"), (2, "host")])
+                                           (3, "device"), ("auto", "device"), (2, "host")])
 @pytest.mark.parametrize("name", FINDER_CASES)
 def test_finder_tables_match_reference(name, mode, epilogue):
     case = Case(name)
@@ -199,10 +199,22 @@ def test_indexed_modes_every_k_equal_oracle(k):
     try:
         plan = f._plan(seqs, pams)
         tunings = [(0, 0, 0), (1024, 32, 0), (2048, 64, 2), (1024, 128, 1)]
-        for mode, tune in [(2, (0, 0, 0)), (2, (0, 0, 0, 1))] + [(3, t) for t in tunings]:
+        seed = [(0, 0, 0), (0, 0, 0, 1), (1024, 0, 0, 0, 4), (0, 0, 2, 1, 4), (1024, 0, 0, 0, 3),
+                (0, 0, 0, 0, 0, 1), (1024, 0, 0, 1, 4, 1), (2048, 0, 0, 1, 3, 1)]
+        for mode, tune in [(2, t) for t in seed] + [(3, t) for t in tunings]:
             plan.set_tuning(*tune)
             got = f._engine.scan(plan, f._strands, [0, 3], k, mode)
             assert got.size == exp.size and np.array_equal(got, exp), (mode, tune)
+        # one launch per family, each family with its own form and tuning
+        plan.set_tuning(0, 0, 0, 1)
+        fam = plan.families()
+        assert fam.min() >= 0 and fam.max() == len(MIXED_PAMS) - 1
+        forms = [dict(form=1), dict(tolerance=1, chunk_sites=1024), dict(min_blocks=4),
+                 dict(tolerance=1, min_blocks=4), dict(chunk_sites=1024)]
+        for fi in range(fam.max() + 1):
+            plan.set_family_tuning(fi, **forms[fi % len(forms)])
+        got = f._engine.scan(plan, f._strands, [0, 3], k, 2)
+        assert np.array_equal(got, exp), "per-family"
         plan.close()
     finally:
         f.close()
