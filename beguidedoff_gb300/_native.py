@@ -29,6 +29,7 @@ EXPORTED = [
     "bgo_epilogue_run", "bgo_synth_genome_repeats", "bgo_engine_transfer",
     "bgo_plan_set_tuning", "bgo_epilogue_fetch", "bgo_scan_time", "bgo_stream_create",
     "bgo_stream_destroy", "bgo_plan_families", "bgo_plan_set_family_tuning",
+    "bgo_genome_upload",
 ]
 
 INPUT_ROW_DTYPE = np.dtype([("plan_row", "<i4"), ("window_mask", "<u4"), ("target_base", "<i4"),
@@ -87,6 +88,7 @@ _SIGS = {
     "bgo_stream_create": ([ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "bgo_stream_destroy": ([_P], ctypes.c_int),
     "bgo_plan_families": ([_P, _P], ctypes.c_int),
+    "bgo_genome_upload": ([_P, _P, _I64, _P, _I64, _P], ctypes.c_int),
     "bgo_plan_set_family_tuning": ([_P, _I32, _P], ctypes.c_int),
     "bgo_scan_time": ([_P, _P, _P, _P, _I32, _I32, _I32, _I32, _P,
                        ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
@@ -258,6 +260,15 @@ class Strand:
         self.handle = h
         self.total_bp = int(total_bp)
         self.device = int(device)
+
+    def upload(self, packed, n_mask_le=None, stream=None):
+        """Replace the contents in place (same total_bp), queued on `stream`
+        (bgo_genome_upload); the arrays must stay valid until the stream
+        has run the copies."""
+        packed = np.ascontiguousarray(packed, dtype=np.uint32)
+        nm = None if n_mask_le is None else np.ascontiguousarray(n_mask_le, dtype=np.uint8)
+        check(lib().bgo_genome_upload(self.handle, ptr(packed), packed.size, ptr(nm),
+                                      0 if nm is None else nm.size, stream), "bgo_genome_upload")
 
     def info(self):
         tb, hn, nb = ctypes.c_int64(), ctypes.c_int(), ctypes.c_int64()

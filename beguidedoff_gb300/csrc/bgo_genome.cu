@@ -111,9 +111,46 @@ extern "C" int bgo_genome_create(const uint32_t *packed, int64_t n_words, int64_
     return BGO_OK;
 }
 
+extern "C" int bgo_genome_upload(bgo_genome *g, const uint32_t *packed, int64_t n_words,
+                                 const uint8_t *n_mask_le, int64_t n_mask_bytes, void *stream) {
+    using namespace bgo;
+    if (!g || !packed || n_words * 16 < g->total_bp || n_mask_bytes < 0 ||
+        ((n_mask_le && n_mask_bytes > 0) ? 1 : 0) != g->has_n) {
+        set_error("bgo_genome_upload: the arrays must cover the genome's total_bp and keep "
+                  "its N-mask presence");
+        return BGO_ERR_ARG;
+    }
+    BGO_CUDA(cudaSetDevice(g->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t need = (size_t)n_words * sizeof(uint32_t) + (size_t)n_mask_bytes + 256;
+    if (need > g->stage_bytes) {
+        BGO_CUDA(cudaStreamSynchronize(s));
+        if (g->d_stage) cudaFree(g->d_stage);
+        g->d_stage = nullptr;
+        g->stage_bytes = 0;
+        BGO_CUDA(cudaMalloc(&g->d_stage, need));
+        g->stage_bytes = need;
+    }
+    uint32_t *d_packed = reinterpret_cast<uint32_t *>(g->d_stage);
+    uint8_t *d_mask = g->has_n ? g->d_stage + ((size_t)n_words * sizeof(uint32_t) + 255) / 256 * 256
+                               : nullptr;
+    BGO_CUDA(cudaMemcpyAsync(d_packed, packed, (size_t)n_words * sizeof(uint32_t),
+                             cudaMemcpyHostToDevice, s));
+    if (g->has_n)
+        BGO_CUDA(cudaMemcpyAsync(d_mask, n_mask_le, (size_t)n_mask_bytes, cudaMemcpyHostToDevice, s));
+    const int threads = 256;
+    const int64_t blocks = ceil_div(g->plane_words, threads);
+    planes_from_packed_kernel<<<(unsigned)blocks, threads, 0, s>>>(
+        d_packed, n_words, d_mask, g->has_n ? n_mask_bytes : 0, g->total_bp, g->plane_words,
+        g->d_planes);
+    BGO_CUDA(cudaGetLastError());
+    return BGO_OK;
+}
+
 extern "C" int bgo_genome_destroy(bgo_genome *genome) {
     if (!genome) return BGO_OK;
     cudaSetDevice(genome->device);
+    if (genome->d_stage) cudaFree(genome->d_stage);
     cudaError_t e = genome->d_planes ? cudaFree(genome->d_planes) : cudaSuccess;
     delete genome;
     if (e != cudaSuccess) return bgo::cuda_fail(e, "bgo_genome_destroy");

@@ -192,6 +192,8 @@ struct bgo_genome {
     int64_t plane_words;
     uint32_t *d_planes;  // [3][plane_words]
     int64_t bytes;
+    unsigned char *d_stage = nullptr;  // packed words + N mask of bgo_genome_upload
+    size_t stage_bytes = 0;
 };
 
 struct bgo_plan {

@@ -75,6 +75,15 @@ int bgo_host_free(void *ptr);
 int bgo_genome_create(const uint32_t *packed, int64_t n_words, int64_t total_bp,
                       const uint8_t *n_mask_le, int64_t n_mask_bytes, int device,
                       void *stream, bgo_genome **out);
+/*
+ * Replaces a strand's contents with new arrays of the same total_bp (and the
+ * same N-mask presence), reusing its device buffers: the copies and the
+ * conversion are queued on `stream` with no allocation and no host
+ * synchronisation.  No reference counterpart: the reference uploads a genome
+ * once and keeps it (beguidedoff/finder.py:321-377).
+ */
+int bgo_genome_upload(bgo_genome *genome, const uint32_t *packed, int64_t n_words,
+                      const uint8_t *n_mask_le, int64_t n_mask_bytes, void *stream);
 int bgo_genome_destroy(bgo_genome *genome);
 /* total_bp, whether an N mask is present, and the device bytes held. */
 int bgo_genome_info(const bgo_genome *genome, int64_t *total_bp, int *has_n_mask,

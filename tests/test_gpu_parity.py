@@ -369,6 +369,29 @@ def test_graph_recaptures_after_hit_buffer_grows():
         f.close()
 
 
+def test_strand_upload_in_place_equals_fresh_strands():
+    """bgo_genome_upload replaces a resident strand's contents without
+    reallocating: scans afterwards see only the new genome."""
+    g1, rng = _random_genome(61, [300_000, 200_001])
+    g2, _ = _random_genome(62, [300_000, 200_001])
+    seqs = ["".join(rng.choice(list("ACGT"), 20)) for _ in range(12)]
+    for s_ in seqs:
+        _plant(g2, rng, s_, "NGG", 4, 3)
+    pams = ["NGG"] * len(seqs)
+    f = beguidedoff(None, max_mismatches=4, genome_data=g1)
+    try:
+        before = f._scan(seqs, pams)
+        assert np.array_equal(before, oracle_keys(g1, seqs, pams, 4))
+        m_fwd, m_rc = prepare_n_masks(g2)
+        for st, arr, m in zip(f._strands, (g2["genome_forward"], g2["genome_rc"]), (m_fwd, m_rc)):
+            st.upload(arr, m)
+        f._strand_arrays = [g2["genome_forward"], g2["genome_rc"]]
+        got = f._scan(seqs, pams)
+        assert np.array_equal(got, oracle_keys(g2, seqs, pams, 4))
+    finally:
+        f.close()
+
+
 def test_large_genome_sampled_ranges_equal_oracle():
     """96 Mbp, 64 NGG guides: full GPU key set; the oracle re-scans four
     sampled 300 kbp ranges per strand and every planted site is found."""
