@@ -46,6 +46,8 @@ _LOGGER = logging.getLogger("beguidedoff")
 _DEFAULT_RESULTS_PER_GUIDE = 10240
 _MAX_RESULTS_PER_GUIDE = 2_621_440
 _DECODE = np.array(list("ACGT"))
+# up to this many chromosomes the device order key holds the name rank exactly
+_EXACT_ORDER_CHROMS = 1024
 _PROFILES = str(Path(__file__).resolve().parent / "base_editor_profiles.tsv")
 
 
@@ -358,6 +360,12 @@ class beguidedoff:
                             hit_keys = np.unique(recs["key"][rec_off[r0]:rec_off[r0 + nr]])
                             pre = (limit, below_by_id if r["count_score_threshold"] is not None
                                    else None)
+                    if pre is not None and len(self.chrom_names) <= _EXACT_ORDER_CHROMS:
+                        r0, nr = spans[i]
+                        out.append(self._table_from_records(
+                            recs[rec_off[r0]:rec_off[r0 + nr]], r0, owners[i], r["guides"],
+                            plan_items, r["return_all"], pre[1]))
+                        continue
                     if pre is None:
                         # a strand hit limit is reached (the genome-order prefix
                         # of every strand is needed) or an editor type is unknown
@@ -369,9 +377,10 @@ class beguidedoff:
                                               r["count_score_threshold"], log, precomputed=pre))
                 except Exception as exc:  # reported to that request only
                     out.append(exc)
+            self.last_batch["epilogue_s"] = (t3 - t2) if parts else 0.0
+            self.last_batch["assemble_s"] = time.perf_counter() - (t3 if parts else t2)
             if info is not None:
-                info["epilogue_s"] = (t3 - t2) if parts else 0.0
-                info["assemble_s"] = time.perf_counter() - (t3 if parts else t2)
+                info.update(self.last_batch)
             return out
         finally:
             plan.close()
@@ -416,7 +425,9 @@ class beguidedoff:
         if input_file is not None:
             guides = load_guides_from_tsv(input_file, presets_path=presets_path or _PROFILES)
         log = logger if logger is not None else _LOGGER
+        t_prep = time.perf_counter()
         keys, mapping = self._prepare(guides)
+        t_prep = time.perf_counter() - t_prep
         if verbose:
             log.info("Guides after deduplication: %d (from %d input rows)", len(keys),
                      len(guides))
@@ -428,6 +439,8 @@ class beguidedoff:
                                     self.max_mismatches, log=log)[0]
             if isinstance(table, Exception):
                 raise table
+            if self.last_batch is not None:
+                self.last_batch["prepare_s"] = t_prep
         else:
             # one plan row per distinct (seq, pam); scan keys that differ only
             # in their on-target share it
@@ -446,6 +459,102 @@ class beguidedoff:
         return table
 
     # ------------------------------------------------------------------
+    def _table_from_records(self, recs, row0, owners, guides, plan_items, return_all,
+                            below_by_id):
+        """Output table straight from the device epilogue's records: each
+        input row's hits among its n_top smallest order keys (score rank,
+        chromosome name rank, local report position, strand - the order of
+        beguidedoff/finder.py:545-566).  Per guide id the rows' records are
+        merged in input-row order, sorted by order key and cut to n_top (all
+        with return_all); every input row of that id then gets the id's
+        table, with its own base editor, as in _assemble."""
+        n_top = self.n_top_offtargets
+        local = recs["input_row"].astype(np.int64) - row0
+        gid_code: Dict[str, int] = {}
+        row_code = np.array([gid_code.setdefault(gid, len(gid_code)) for gid in owners],
+                            dtype=np.int64)
+        rec_code = row_code[local] if local.size else np.zeros(0, dtype=np.int64)
+        # ties (possible only between identical hits of rows sharing a plan
+        # row) keep _assemble's order: input row, then hit key
+        order = np.lexsort((recs["key"], local, recs["order"], rec_code))
+        codes_sorted = rec_code[order]
+        first = np.searchsorted(codes_sorted, codes_sorted, side="left")
+        rank = np.arange(order.size) - first
+        keep = order if return_all else order[rank < n_top]
+        kcode = rec_code[keep]
+        # per guide id: its kept records, in order
+        bounds = np.searchsorted(kcode, np.arange(len(gid_code) + 1), side="left")
+        # decode the kept hits (vectorised)
+        row, slot, pos, mm = _native.split_keys(recs["key"][keep])
+        n = keep.size
+        seq = np.zeros((n, 20), dtype=np.uint8)
+        pam = np.zeros((n, 6), dtype=np.uint8)
+        for st in range(len(self._strand_arrays)):
+            sel = np.nonzero(slot == st)[0]
+            if sel.size:
+                arr = self._strand_arrays[st]
+                seq[sel] = extract_windows(arr, pos[sel], 20)
+                pam[sel] = extract_windows(arr, pos[sel] + 20, 6)
+        plen = np.array([len(plan_items[r][1]) for r in row.tolist()], dtype=np.int64)
+        gb = np.zeros((len(plan_items), 20), dtype=np.uint8)
+        for p_i, (gseq, _) in enumerate(plan_items):
+            enc = encode_dna(gseq)[:20]
+            gb[p_i, :enc.size] = enc
+        weights = np.int64(1) << np.arange(20, dtype=np.int64)
+        mmask = ((seq != gb[row]).astype(np.int64) * weights[None, :]).sum(1) if n else \
+            np.zeros(0, dtype=np.int64)
+        score = cctop_from_masks(mmask)
+        offsets, lengths = self.chrom_offsets, self.chrom_lengths
+        window = 20 + plen
+        leftmost = pos.copy()
+        minus = slot == 1
+        if minus.any():
+            ci = np.searchsorted(offsets, pos[minus], side="right") - 1
+            leftmost[minus] = offsets[ci] + (lengths[ci] - (pos[minus] - offsets[ci]) - window[minus])
+        report = np.where(minus, leftmost + window - 1, pos)
+        rep_ci = np.searchsorted(offsets, report, side="right") - 1
+        rep_local = report - offsets[rep_ci]
+        # one block per input guide row, in input order
+        blocks, editors, below = [], [], []
+        for g in guides:
+            c = gid_code.get(g.guide_id)
+            if c is None or bounds[c] == bounds[c + 1]:
+                continue
+            blocks.append(np.arange(bounds[c], bounds[c + 1]))
+            editors.append(g.base_editor or "")
+            below.append((below_by_id or {}).get(g.guide_id, 0))
+        if not blocks:
+            if pandas_available():
+                import pandas as pd
+
+                return pd.DataFrame()
+            return Table()
+        sizes = np.array([b.size for b in blocks], dtype=np.int64)
+        idx = np.concatenate(blocks)
+        seq_s = ["".join(r) for r in _DECODE[seq[idx]]]
+        pam_s = ["".join(r[:k]) for r, k in zip(_DECODE[pam[idx]], plen[idx].tolist())]
+        mpos = [",".join(str(i + 1) for i in range(20) if (m >> i) & 1)
+                for m in mmask[idx].tolist()]
+        cols = {
+            "guide_rna_sequence": np.array([plan_items[r][0] for r in row[idx].tolist()],
+                                           dtype=object),
+            "base_editor": np.repeat(np.array(editors, dtype=object), sizes),
+            "ot_rank": np.concatenate([np.arange(1, k + 1, dtype=np.int64) for k in sizes]),
+            "ot_chromosome": np.array([self.chrom_names[c] for c in rep_ci[idx].tolist()],
+                                      dtype=object),
+            "ot_position": (rep_local[idx] + 1).astype(np.int64),
+            "ot_strand": np.where(slot[idx] == 1, "-", "+").astype(object),
+            "ot_sequence": np.array(seq_s, dtype=object),
+            "ot_pam": np.array(pam_s, dtype=object),
+            "n_mismatches": mm[idx].astype(np.int64),
+            "mismatch_positions": np.array(mpos, dtype=object),
+            "score": np.array([round(float(v), 6) for v in score[idx].tolist()],
+                              dtype=np.float64),
+            "n_offtargets_below_threshold": np.repeat(np.array(below, dtype=np.int64), sizes),
+        }
+        t = Table(cols, COLUMNS)
+        return t.to_pandas() if pandas_available() else t
+
     def _assemble(self, hit_keys, keys, key_plan, plan_items, mapping, guides, return_all,
                   count_score_threshold, log, precomputed=None):
         """Output table from sorted hit keys.  ``precomputed`` = (per-key

@@ -546,6 +546,8 @@ def bench_ours(args, ws, rank, local):
                     "rows": len(table), "launches": e2e_launches // args.steps,
                     "genome": "resident between searches, as the reference keeps it"},
             "e2e_genome_upload": e2e_up,
+            "e2e_split_s": {k: round(v, 5) for k, v in (f.last_batch or {}).items()
+                            if k.endswith("_s")},
             "gpu_launches": launches,
             "tuning": getattr(plan, "tuning", None),
             "autotune": autotune,
