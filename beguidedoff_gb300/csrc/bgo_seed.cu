@@ -49,16 +49,21 @@ size_t seed_smem_bytes(const SeedArgs &sa, int chunk_sites) {
 
 int launch_seed_t1(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
                    int min_blocks, int ctas_per_sm, cudaStream_t s);
+int launch_seed_t0i2(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
+                     int min_blocks, int ctas_per_sm, cudaStream_t s);
 
 int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
-                       int min_blocks, int tolerance, int ctas_per_sm, cudaStream_t s) {
+                       int min_blocks, int tolerance, int inline_entries, int ctas_per_sm,
+                       cudaStream_t s) {
     if (chunk_sites != 1024 && chunk_sites != 2048) {
         set_error("segment index: chunk_sites must be 1024 or 2048");
         return BGO_ERR_ARG;
     }
     if (tolerance == 1)
         return launch_seed_t1(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
-    return launch_tol<0>(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
+    if (inline_entries == 2)
+        return launch_seed_t0i2(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
+    return launch_form<0, 1>(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
 }
 
 // PAM test program of a family: one test per constrained position (an N is

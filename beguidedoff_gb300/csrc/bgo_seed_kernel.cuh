@@ -1,6 +1,7 @@
 // Segment-indexed scan kernel (scan mode 2), included by the translation
-// units that instantiate it for tolerance 0 (bgo_seed.cu) and tolerance 1
-// (bgo_seed_t1.cu), which compile in parallel.  The algorithm is described at
+// units that instantiate its forms - tolerance 0 with one inline guide per
+// bucket (bgo_seed.cu), tolerance 0 with two (bgo_seed_i2.cu), tolerance 1
+// with two (bgo_seed_t1.cu) - so that they compile in parallel.  The algorithm is described at
 // the top of bgo_seed.cu.
 #pragma once
 
@@ -75,7 +76,7 @@ __device__ __noinline__ void finish_candidate(const ScanParams &p, uint32_t m, i
           p.counter);
 }
 
-template <int K, int TOL, int CH, int MINB>
+template <int K, int TOL, int INLINE, int CH, int MINB>
 __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParams p, SeedArgs sa) {
     using G = SegT<K, TOL>;
     constexpr int S = G::S;
@@ -227,8 +228,11 @@ __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParam
                 // bucket compares its region list's first entry, always
                 // present, and ignores the result), (3) the rare candidates
                 // within K.  Further guides of a bucket stay as a range.
+                // INLINE (1 or 2) guides of each bucket are compared inline;
+                // the rest of a bucket goes through the queue
+                constexpr uint32_t INL = (uint32_t)INLINE;
                 uint32_t rn[S], e0v[S];
-                uint32_t T = 0, R = 0, within = 0;
+                uint32_t T = 0, R = 0, within = 0, within2 = 0;
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
                     const int st = G::start(j), kl = G::klen(j);
@@ -238,24 +242,34 @@ __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParam
                     const uint32_t n = d >> 16;
                     e0v[j] = seg_ent[j] + (d & 0xFFFFu);
                     T += n;
-                    rn[j] = n > 1u ? n - 1u : 0u;
+                    rn[j] = n > INL ? n - INL : 0u;
                     R += rn[j] != 0u;
                     if (n == 0u) e0v[j] = seg_ent[j];
                     within |= (n != 0u ? 1u : 0u) << j;
+                    if (INL == 2u) within2 |= (n >= 2u ? 1u : 0u) << j;
                 }
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
                     const uint2 e = sEnt[e0v[j]];
                     if (__popc((h20 ^ e.x) | (l20 ^ e.y)) > K) within &= ~(1u << j);
+                    if (INL == 2u) {
+                        // the second entry (the first again when the bucket holds one)
+                        const uint2 e2 = sEnt[e0v[j] + ((within2 >> j) & 1u)];
+                        if (__popc((h20 ^ e2.x) | (l20 ^ e2.y)) > K) within2 &= ~(1u << j);
+                    }
                 }
-                if (within) {
+                if (within | within2) {
 #pragma unroll
                     for (int j = 0; j < S; ++j) {
-                        if (within & (1u << j)) {
-                            const uint2 e = sEnt[e0v[j]];
-                            const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
-                            finish_candidate<K, TOL>(p, m, __popc(m), e, sIdx[e0v[j]], j, n20g,
-                                                     ne, slot, pos, gbeg);
+#pragma unroll
+                        for (uint32_t a = 0; a < INL; ++a) {
+                            if (((a == 0u ? within : within2) >> j) & 1u) {
+                                const uint32_t ei = e0v[j] + a;
+                                const uint2 e = sEnt[ei];
+                                const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
+                                finish_candidate<K, TOL>(p, m, __popc(m), e, sIdx[ei], j, n20g,
+                                                         ne, slot, pos, gbeg);
+                            }
                         }
                     }
                 }
@@ -274,7 +288,7 @@ __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParam
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
                     if (rn[j]) {
-                        wQ[qp] = (e0v[j] + 1u) | ((uint32_t)j << 22) | ((uint32_t)lane << 27);
+                        wQ[qp] = (e0v[j] + INL) | ((uint32_t)j << 22) | ((uint32_t)lane << 27);
                         wCnt[qp] = (uint16_t)rn[j];
                         ++qp;
                     }
@@ -307,56 +321,56 @@ __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParam
     if (t == 0 && sCand) atomicAdd(p.counter + 1, sCand);
 }
 
-template <int K, int TOL, int CH, int MINB>
+template <int K, int TOL, int INLINE, int CH, int MINB>
 static int launch_k(const ScanParams &p, const SeedArgs &sa, int sm_count, int ctas_per_sm,
                     cudaStream_t s) {
     const size_t smem = seed_smem_bytes(sa, CH);
     static size_t configured = 0;
     if (smem > configured) {
-        BGO_CUDA(cudaFuncSetAttribute(scan_seed_kernel<K, TOL, CH, MINB>,
+        BGO_CUDA(cudaFuncSetAttribute(scan_seed_kernel<K, TOL, INLINE, CH, MINB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
     }
     int per_sm = 0;
     BGO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, scan_seed_kernel<K, TOL, CH, MINB>, kSeedThreads, smem));
+        &per_sm, scan_seed_kernel<K, TOL, INLINE, CH, MINB>, kSeedThreads, smem));
     if (per_sm < 1) per_sm = 1;
     if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
     const int64_t blocks_needed = (p.tiles_total + kSeedWarps - 1) / kSeedWarps;
     const int64_t grid = std::min<int64_t>(blocks_needed, (int64_t)sm_count * per_sm);
-    scan_seed_kernel<K, TOL, CH, MINB><<<(unsigned)grid, kSeedThreads, smem, s>>>(p, sa);
+    scan_seed_kernel<K, TOL, INLINE, CH, MINB><<<(unsigned)grid, kSeedThreads, smem, s>>>(p, sa);
     BGO_CUDA(cudaGetLastError());
     return BGO_OK;
 }
 
-template <int TOL, int CH, int MINB>
+template <int TOL, int INLINE, int CH, int MINB>
 static int launch_cm(const ScanParams &p, const SeedArgs &sa, int sm_count, int ctas_per_sm,
                      cudaStream_t s) {
     switch (p.max_mm) {
-        case 0: return launch_k<0, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 1: return launch_k<1, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 2: return launch_k<2, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 3: return launch_k<3, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 4: return launch_k<4, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 5: return launch_k<5, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 6: return launch_k<6, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 7: return launch_k<7, TOL, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 0: return launch_k<0, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 1: return launch_k<1, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 2: return launch_k<2, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 3: return launch_k<3, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 4: return launch_k<4, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 5: return launch_k<5, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 6: return launch_k<6, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 7: return launch_k<7, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
         default:
             set_error("segment index: max_mismatches outside 0..7");
             return BGO_ERR_ARG;
     }
 }
 
-// All chunk lengths and occupancy targets for one tolerance.
-template <int TOL>
-static int launch_tol(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
-                      int min_blocks, int ctas_per_sm, cudaStream_t s) {
+// All chunk lengths and occupancy targets for one (tolerance, inline) form.
+template <int TOL, int INLINE>
+static int launch_form(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
+                       int min_blocks, int ctas_per_sm, cudaStream_t s) {
     const bool c1k = chunk_sites == 1024;
     if (min_blocks == 4)
-        return c1k ? launch_cm<TOL, 1024, 4>(p, sa, sm_count, ctas_per_sm, s)
-                   : launch_cm<TOL, 2048, 4>(p, sa, sm_count, ctas_per_sm, s);
-    return c1k ? launch_cm<TOL, 1024, 3>(p, sa, sm_count, ctas_per_sm, s)
-               : launch_cm<TOL, 2048, 3>(p, sa, sm_count, ctas_per_sm, s);
+        return c1k ? launch_cm<TOL, INLINE, 1024, 4>(p, sa, sm_count, ctas_per_sm, s)
+                   : launch_cm<TOL, INLINE, 2048, 4>(p, sa, sm_count, ctas_per_sm, s);
+    return c1k ? launch_cm<TOL, INLINE, 1024, 3>(p, sa, sm_count, ctas_per_sm, s)
+               : launch_cm<TOL, INLINE, 2048, 3>(p, sa, sm_count, ctas_per_sm, s);
 }
 
 }  // namespace bgo

@@ -158,6 +158,9 @@ int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
  *   tolerance     mode 2: mismatches allowed in a key region, 0 (K + 1 exact
  *                 regions) or 1 (K / 2 + 1 regions, guides also indexed under
  *                 every single-base substitution of their keys)
+ *   inline_entries  mode 2, tolerance 0: guides of each bucket compared inline
+ *                 before the range queue, 1 or 2 (0 = 1); tolerance 1 always
+ *                 compares 2
  * Changing group_guides rebuilds the mask index at the next launch.  No
  * reference counterpart: the reference fixes 256 threads x 200 Mbp chunks.
  */
@@ -169,7 +172,7 @@ typedef struct bgo_tuning {
     int32_t min_blocks;
     int32_t tolerance;
     int32_t family_form;   /* per-family tuning only: 0 segment index, 1 compare every guide */
-    int32_t reserved;
+    int32_t inline_entries;
 } bgo_tuning;
 int bgo_plan_set_tuning(bgo_plan *plan, const bgo_tuning *tuning);
 
