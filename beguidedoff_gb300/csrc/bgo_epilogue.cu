@@ -82,6 +82,31 @@ struct EpiParams {
     bgo_record *recs;
 };
 
+// atomicAdd of 1 per lane, aggregated over the active lanes that target the
+// same address (one atomic per distinct address per warp: hits of one dense
+// guide land on the same few counters).
+template <typename T>
+__device__ __forceinline__ void aggregated_inc(T *addr) {
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, (unsigned long long)addr);
+    const int leader = __ffs(peers) - 1;
+    if ((int)(threadIdx.x & 31) == leader) atomicAdd(addr, (T)__popc(peers));
+}
+
+// Fetch-and-increment with the same aggregation: every lane gets its own
+// slot (the peers' base plus its rank among them).
+template <typename T>
+__device__ __forceinline__ T aggregated_fetch_inc(T *addr) {
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, (unsigned long long)addr);
+    const int leader = __ffs(peers) - 1;
+    const int lane = (int)(threadIdx.x & 31);
+    T base = 0;
+    if (lane == leader) base = atomicAdd(addr, (T)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + (T)__popc(peers & ((1u << lane) - 1u));
+}
+
 // Index of the last chromosome whose offset is <= pos (-1 below the first,
 // like Python's searchsorted(..., 'right') - 1).
 __device__ __forceinline__ int chrom_of(const int64_t *off, int n, int64_t pos) {
@@ -126,7 +151,7 @@ __global__ void epilogue_kernel(EpiParams e) {
         const int ot_ci = chrom_of(off, nc, leftmost);
         // Python indexes chromosome -1 as the last one
         const int64_t ot_local = leftmost - off[ot_ci >= 0 ? ot_ci : nc - 1];
-        if (PASS == 1) atomicAdd(e.group_cnt + 2 * row + slot, 1ull);
+        if (PASS == 1) aggregated_inc(e.group_cnt + 2 * row + slot);
         uint64_t order = (uint64_t)rank << 44;
         if (PASS == 2 && e.exact_order) {
             const int64_t report = slot ? leftmost + window - 1 : pos;
@@ -148,10 +173,10 @@ __global__ void epilogue_kernel(EpiParams e) {
             const uint32_t bin = rank >> kRankShift;
             if (PASS == 1) {
                 if (in.threshold_rank >= 0 && editable && (int32_t)rank <= in.threshold_rank)
-                    atomicAdd(e.below + ir, 1ull);
-                if (include) atomicAdd(e.hist + (size_t)ir * kRankBins + bin, 1u);
+                    aggregated_inc(e.below + ir);
+                if (include) aggregated_inc(e.hist + (size_t)ir * kRankBins + bin);
             } else if (include && (int32_t)bin <= e.cut[ir]) {
-                const unsigned long long f = atomicAdd(e.fill + ir, 1ull);
+                const unsigned long long f = aggregated_fetch_inc(e.fill + ir);
                 if ((int64_t)f < e.seg_cnt[ir]) {
                     bgo_record r;
                     r.key = key;

@@ -481,6 +481,7 @@ def bench_ours(args, ws, rank, local):
     e2e_launches = eng.launch_count() - n1
     h2d = (x1["h2d"] - x0["h2d"]) // args.steps
     d2h = (x1["d2h"] - x0["d2h"]) // args.steps
+    e2e_split = {k: round(v, 5) for k, v in (f.last_batch or {}).items() if k.endswith("_s")}
 
     # (b) conservative: both strand arrays and N masks also uploaded from
     #     pinned host memory every step, into the same device buffers
@@ -546,8 +547,7 @@ def bench_ours(args, ws, rank, local):
                     "rows": len(table), "launches": e2e_launches // args.steps,
                     "genome": "resident between searches, as the reference keeps it"},
             "e2e_genome_upload": e2e_up,
-            "e2e_split_s": {k: round(v, 5) for k, v in (f.last_batch or {}).items()
-                            if k.endswith("_s")},
+            "e2e_split_s": e2e_split,
             "gpu_launches": launches,
             "tuning": getattr(plan, "tuning", None),
             "autotune": autotune,
