@@ -118,7 +118,10 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def dist_setup():
+def dist_setup(backend=None):
+    """Rank layout from the torchrun environment; for WORLD_SIZE > 1 a process
+    group over NCCL (one GPU per rank), or the given backend (gloo in the CPU
+    tests).  The scan shards as replicas: no collective on the data path."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -126,18 +129,22 @@ def dist_setup():
         import torch
         import torch.distributed as dist
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend is None:
+            backend = "nccl"
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return ws, rank, local
 
 
 def dist_max(x, ws):
+    """Maximum of x over the ranks (the slowest rank's time)."""
     if ws <= 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -147,6 +154,12 @@ def barrier(ws):
         import torch.distributed as dist
 
         dist.barrier()
+
+
+def replica_value(ws, units_per_rank, t_max_s):
+    """Whole-job throughput of N replicas: all ranks' units over the slowest
+    rank's time (weak scaling)."""
+    return ws * units_per_rank / t_max_s
 
 
 MIXED_FAMILIES = (("NGG", 0.40), ("NG", 0.20), ("NNGRRT", 0.15), ("NNNRRT", 0.15),
@@ -515,7 +528,7 @@ def bench_ours(args, ws, rank, local):
                "sample": sample + f" ({dt:.1f} s, oracle/scan_oracle.c OpenMP)"}
 
     if rank == 0:
-        value = ws * comps / (t_max / args.steps)
+        value = replica_value(ws, comps, t_max / args.steps)
         popc = {"achieved_gops": achieved, "peak_gops": popc_peak, "frac": achieved / popc_peak,
                 "compares_per_step": pairs, "lop3_peak_gops": lop3_peak,
                 "peak_source": "measured live: bgo_probe_int_throughput"}
