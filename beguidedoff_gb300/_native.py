@@ -29,7 +29,7 @@ EXPORTED = [
     "bgo_epilogue_run", "bgo_synth_genome_repeats", "bgo_engine_transfer",
     "bgo_plan_set_tuning", "bgo_epilogue_fetch", "bgo_scan_time", "bgo_stream_create",
     "bgo_stream_destroy", "bgo_plan_families", "bgo_plan_set_family_tuning",
-    "bgo_genome_upload",
+    "bgo_genome_upload", "bgo_encode_genome",
 ]
 
 INPUT_ROW_DTYPE = np.dtype([("plan_row", "<i4"), ("window_mask", "<u4"), ("target_base", "<i4"),
@@ -89,6 +89,7 @@ _SIGS = {
     "bgo_stream_destroy": ([_P], ctypes.c_int),
     "bgo_plan_families": ([_P, _P], ctypes.c_int),
     "bgo_genome_upload": ([_P, _P, _I64, _P, _I64, _P], ctypes.c_int),
+    "bgo_encode_genome": ([_P, _P, _I32, ctypes.c_int, _P, _P, _P], ctypes.c_int),
     "bgo_plan_set_family_tuning": ([_P, _I32, _P], ctypes.c_int),
     "bgo_scan_time": ([_P, _P, _P, _P, _I32, _I32, _I32, _I32, _P,
                        ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
@@ -165,6 +166,27 @@ def synth_genome(seed, chrom_lengths, n_blocks=(), thresholds=(64, 128, 192), de
         out["repeat_families"] = ["".join("ACGT"[b] for b in r)
                                   for r in fams.reshape(spec.n_families, spec.family_len)]
     return out
+
+
+def encode_genome(seq: bytes, chrom_lengths, include_rc=True, include_n_mask=True, device=0):
+    """(forward words, reverse-complement words or None, big-endian N mask or
+    None) of concatenated sequence bytes, encoded on the device
+    (bgo_encode_genome)."""
+    lens = np.ascontiguousarray(chrom_lengths, dtype=np.int64)
+    total = int(lens.sum())
+    raw = np.frombuffer(seq, dtype=np.uint8) if total else np.zeros(1, dtype=np.uint8)
+    if raw.size < total:
+        raise ValueError("sequence shorter than the chromosome lengths")
+    n_words, n_bytes = (total + 15) // 16, (total + 7) // 8
+    fwd = np.zeros(n_words, dtype=np.uint32)
+    rc = np.zeros(n_words, dtype=np.uint32) if include_rc else None
+    nm = np.zeros(n_bytes, dtype=np.uint8) if include_n_mask else None
+    check(lib().bgo_encode_genome(raw.ctypes.data, ptr(lens), lens.size, int(device),
+                                  fwd.ctypes.data if n_words else None,
+                                  None if rc is None or not n_words else rc.ctypes.data,
+                                  None if nm is None or not n_bytes else nm.ctypes.data),
+          "bgo_encode_genome")
+    return fwd, rc, nm
 
 
 def probe_int_throughput(op, device=0):

@@ -10,7 +10,7 @@ unmasked).  The reference walks every base in Python; here each chromosome
 is one table lookup.
 """
 from pathlib import Path
-from typing import Dict, List, Tuple
+from typing import Dict, List, Optional, Tuple
 
 import numpy as np
 
@@ -36,7 +36,13 @@ def read_fasta(path: str) -> List[Tuple[str, bytes]]:
     return out
 
 
-def encode_chromosomes(chroms: List[Tuple[str, bytes]], include_rc=True, include_n_mask=True):
+def encode_chromosomes(chroms: List[Tuple[str, bytes]], include_rc=True, include_n_mask=True,
+                       device: Optional[int] = None):
+    """The .npz arrays of (name, sequence) pairs; on the GPU (bgo_encode_genome)
+    when ``device`` is a CUDA device index, else vectorised NumPy.  Both give
+    the same bytes."""
+    if device is not None and chroms and sum(len(seq) for _, seq in chroms):
+        return _encode_on_device(chroms, include_rc, include_n_mask, device)
     names, offsets, lengths = [], [], []
     fwd, rc, nmask = [], [], []
     off = 0
@@ -68,11 +74,32 @@ def encode_chromosomes(chroms: List[Tuple[str, bytes]], include_rc=True, include
     return out
 
 
+def _encode_on_device(chroms, include_rc, include_n_mask, device):
+    from . import _native
+
+    lengths = np.array([len(seq) for _, seq in chroms], dtype=np.int64)
+    fwd, rc, nm = _native.encode_genome(b"".join(seq for _, seq in chroms), lengths,
+                                        include_rc, include_n_mask, device)
+    out: Dict[str, np.ndarray] = {
+        "genome_forward": fwd,
+        "chrom_names": np.array([name for name, _ in chroms]),
+        "chrom_offsets": np.concatenate([[0], np.cumsum(lengths)[:-1]]).astype(np.int64)
+        if lengths.size else np.zeros(0, dtype=np.int64),
+        "chrom_lengths": lengths,
+        "total_bp": np.int64(lengths.sum()),
+    }
+    if include_rc:
+        out["genome_rc"] = rc
+    if include_n_mask:
+        out["n_mask"] = nm
+    return out
+
+
 def convert(fasta_path: str, output_path: str, include_rc: bool = True,
             include_n_mask: bool = True, chunk_size: int = 100_000_000,
-            verbose: bool = True) -> None:
+            verbose: bool = True, device: Optional[int] = None) -> None:
     chroms = read_fasta(fasta_path)
-    data = encode_chromosomes(chroms, include_rc, include_n_mask)
+    data = encode_chromosomes(chroms, include_rc, include_n_mask, device)
     if verbose:
         print(f"  Total genome: {int(data['total_bp']):,} bp")
     np.savez_compressed(output_path, **data)

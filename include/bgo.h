@@ -327,6 +327,17 @@ int bgo_scan_noalloc(const bgo_genome *const *strands, const int32_t *n_encoded,
                      void *stream);
 
 /*
+ * FASTA sequence bytes (all chromosomes concatenated, in file order) -> the
+ * reference's .npz arrays on the device, as beguidedoff/genome_converter.py
+ * :15-108 writes them: fwd_out ceil(total/16) words; rc_out (optional) the
+ * per-chromosome reverse complement in the same layout; n_mask_big_out
+ * (optional) ceil(total/8) bytes, N/n positions, np.packbits bit order.  Only
+ * A/C/G/T (either case) have non-zero codes.
+ */
+int bgo_encode_genome(const uint8_t *seq, const int64_t *chrom_lengths, int32_t n_chroms,
+                      int device, uint32_t *fwd_out, uint32_t *rc_out, uint8_t *n_mask_big_out);
+
+/*
  * Seeded synthetic genome in the reference .npz layout (what
  * beguidedoff/genome_converter.py:15-108 writes for the equivalent FASTA):
  * chromosomes of the given lengths concatenated, bases drawn per position from

@@ -84,3 +84,49 @@ def _best_alignment(seg, fams):
                 d = int((seg[s0:s0 + cand.size] != cand).sum())
                 best = d if best is None else min(best, d)
     return best
+
+
+def test_gpu_converter_matches_reference_golden(tmp_path):
+    """bgo_encode_genome gives the reference convert()'s bytes (the golden
+    recorded from the reference) for every include_rc / include_n_mask."""
+    import os
+
+    from _golden import GOLDEN_DIR
+    from beguidedoff_gb300 import genome_converter as GC
+
+    d = np.load(os.path.join(GOLDEN_DIR, "convert.npz"))
+    fa = tmp_path / "g.fa"
+    fa.write_text(str(d["fasta_text"]))
+    for rc in (True, False):
+        for nm in (True, False):
+            out = tmp_path / f"o{rc}{nm}.npz"
+            GC.convert(str(fa), str(out), include_rc=rc, include_n_mask=nm, verbose=False,
+                       device=0)
+            got = np.load(out)
+            pre = f"rc{int(rc)}_nm{int(nm)}_"
+            exp_keys = sorted(k[len(pre):] for k in d.files if k.startswith(pre))
+            assert sorted(got.files) == exp_keys
+            for k in exp_keys:
+                assert np.array_equal(got[k], d[pre + k]), (rc, nm, k)
+
+
+def test_gpu_encoder_equals_host_encoder_on_random_fasta():
+    from beguidedoff_gb300 import genome_converter as GC
+
+    rng = np.random.default_rng(12)
+    alphabet = np.frombuffer(b"ACGTacgtNnRYKMSWBDHVx-", dtype=np.uint8)
+    probs = np.array([0.2] * 4 + [0.02] * 4 + [0.05, 0.03] + [0.004] * 12)
+    probs /= probs.sum()
+    chroms = []
+    for i, ln in enumerate([0, 1, 15, 16, 17, 1000, 33_333, 250_001]):
+        seq = rng.choice(alphabet, size=ln, p=probs).astype(np.uint8)
+        if ln > 500:
+            seq[100:300] = ord("N")
+        chroms.append((f"c{i}", seq.tobytes()))
+    for rc in (True, False):
+        for nm in (True, False):
+            host = GC.encode_chromosomes(chroms, rc, nm)
+            dev = GC.encode_chromosomes(chroms, rc, nm, device=0)
+            assert sorted(host) == sorted(dev)
+            for k in host:
+                assert np.array_equal(np.asarray(host[k]), np.asarray(dev[k])), (rc, nm, k)
