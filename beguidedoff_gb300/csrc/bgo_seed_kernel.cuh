@@ -274,8 +274,25 @@ __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParam
                     }
                 }
                 cand += T;
-                // buckets with more than one guide: ranges through the queue
                 if (!__any_sync(0xFFFFFFFFu, R != 0u)) continue;
+                if constexpr (TOL == 1) {
+                    // tolerance-1 buckets rarely hold more than the inline two:
+                    // each lane walks its own few remaining entries
+#pragma unroll
+                    for (int j = 0; j < S; ++j) {
+                        for (uint32_t i = 0; i < rn[j]; ++i) {
+                            const uint32_t ei = e0v[j] + INL + i;
+                            const uint2 e = sEnt[ei];
+                            const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
+                            const int cm = __popc(m);
+                            if (cm <= K)
+                                finish_candidate<K, TOL>(p, m, cm, e, sIdx[ei], j, n20g, ne, slot,
+                                                         pos, gbeg);
+                        }
+                    }
+                    continue;
+                }
+                // buckets with more guides: ranges spread over the warp's lanes
                 uint32_t rin = R;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
