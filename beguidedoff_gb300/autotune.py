@@ -32,6 +32,7 @@ CANDIDATES: Tuple[Tuple[str, int, Tuple[int, ...]], ...] = (
     ("all-guides", 1, (0, 0, 0, 0, 0, 0, 0)),
     ("segment-index", 2, (0, 0, 0, 0, 0, 0, 0)),
     ("segment-index/i2", 2, (0, 0, 0, 0, 0, 0, 2)),
+    ("segment-index/walk", 2, (0, 0, 0, 0, 0, 0, 0, 1)),
     ("segment-index/1024/occ4", 2, (1024, 0, 0, 0, 4, 0, 0)),
     ("segment-index/per-family", 2, (0, 0, 0, 1, 0, 0, 0)),
     ("segment-index/t1", 2, (0, 0, 0, 0, 0, 1, 0)),
@@ -41,20 +42,21 @@ CANDIDATES: Tuple[Tuple[str, int, Tuple[int, ...]], ...] = (
     ("segment-masks/2048x128", 3, (2048, 128, 0, 0, 0, 0, 0)),
 )
 TUNING_FIELDS = ("chunk_sites", "group_guides", "ctas_per_sm", "split_families", "min_blocks",
-                 "tolerance", "inline_entries")
+                 "tolerance", "inline_entries", "range_walk")
 # per PAM family, timed on a plan holding that family alone:
 # (name, form (0 segment index, 1 every guide), chunk_sites, min_blocks, tolerance,
-#  inline_entries)
+#  inline_entries, range_walk)
 FAMILY_CANDIDATES = (
-    ("every-guide", 1, 0, 0, 0, 0),
-    ("index", 0, 0, 0, 0, 0),
-    ("index/i2", 0, 0, 0, 0, 2),
-    ("index/1024/occ4", 0, 1024, 4, 0, 0),
-    ("index/t1", 0, 0, 0, 1, 0),
-    ("index/t1/1024", 0, 1024, 0, 1, 0),
-    ("index/t1/1024/occ4", 0, 1024, 4, 1, 0),
+    ("every-guide", 1, 0, 0, 0, 0, 0),
+    ("index", 0, 0, 0, 0, 0, 0),
+    ("index/walk", 0, 0, 0, 0, 0, 1),
+    ("index/i2", 0, 0, 0, 0, 2, 0),
+    ("index/1024/occ4", 0, 1024, 4, 0, 0, 0),
+    ("index/t1", 0, 0, 0, 1, 0, 0),
+    ("index/t1/1024", 0, 1024, 0, 1, 0, 0),
+    ("index/t1/1024/occ4", 0, 1024, 4, 1, 0, 0),
 )
-PER_FAMILY_TUNING = (0, 0, 0, 1, 0, 0, 0)
+PER_FAMILY_TUNING = (0, 0, 0, 1, 0, 0, 0, 0)
 INDEXED_MAX_K = 7
 
 
@@ -66,14 +68,14 @@ class Choice:
     times_ms: Dict[str, float] = field(default_factory=dict)
     sample_bp: int = 0
     # per-family choice (name "per-family"): PAM -> (name, form, chunk_sites,
-    # min_blocks, tolerance, inline_entries, ms alone)
+    # min_blocks, tolerance, inline_entries, range_walk, ms alone)
     family: Dict[str, tuple] = field(default_factory=dict)
 
     def as_dict(self):
         return {"name": self.name, "mode": self.mode,
                 "tuning": dict(zip(TUNING_FIELDS, self.tuning)),
                 "times_ms": {k: round(v, 4) for k, v in self.times_ms.items()},
-                "family": {p: {"form": c[0], "ms": round(c[6], 4)} for p, c in
+                "family": {p: {"form": c[0], "ms": round(c[7], 4)} for p, c in
                            self.family.items()},
                 "sample_bp": self.sample_bp}
 
@@ -90,7 +92,7 @@ class Choice:
             c = self.family.get(pams[row].upper())
             if c is not None:
                 plan.set_family_tuning(f, chunk_sites=c[2], min_blocks=c[3], tolerance=c[4],
-                                       form=c[1], inline_entries=c[5])
+                                       form=c[1], inline_entries=c[5], range_walk=c[6])
 
 
 def signature(pams: Sequence[str], max_mismatches: int) -> tuple:
@@ -194,16 +196,16 @@ class Autotuner:
                                plan.pam_lens[rows], plan.pam_3prime[rows], stream)
             try:
                 best = None
-                for name, form, chunk, minb, tol, inl in FAMILY_CANDIDATES:
-                    sub.set_tuning(chunk, 0, 0, 0, minb, tol, inl)
+                for name, form, chunk, minb, tol, inl, walk in FAMILY_CANDIDATES:
+                    sub.set_tuning(chunk, 0, 0, 0, minb, tol, inl, walk)
                     ms = self.engine.scan_time(sub, strands, ne, max_mismatches,
                                                1 if form == 1 else 2, self.reps, stream)
-                    if best is None or ms < best[6]:
-                        best = (name, form, chunk, minb, tol, inl, ms)
+                    if best is None or ms < best[7]:
+                        best = (name, form, chunk, minb, tol, inl, walk, ms)
             finally:
                 sub.close()
             out[pams[int(rows[0])].upper()] = best
-            total += best[6]
+            total += best[7]
         return total, out
 
     def close(self):

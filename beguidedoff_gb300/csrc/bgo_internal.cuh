@@ -230,8 +230,8 @@ bool build_seed_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, 
                       std::vector<uint2> &entries, std::vector<uint16_t> &entry_idx);
 size_t seed_smem_bytes(const SeedArgs &sa, int chunk_sites);
 int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
-                       int min_blocks, int tolerance, int inline_entries, int ctas_per_sm,
-                       cudaStream_t s);
+                       int min_blocks, int tolerance, int inline_entries, int range_walk,
+                       int ctas_per_sm, cudaStream_t s);
 void pam_program(const FamilyDesc &F, SeedFam &sf);
 bool build_mask_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
                       int group_max, std::vector<MaskFam> &out_fams,

@@ -405,10 +405,11 @@ static int check_tuning(const bgo_plan *pl, const bgo_tuning *t) {
         t->ctas_per_sm < 0 || t->split_families < 0 || t->split_families > 1 ||
         (t->min_blocks != 0 && t->min_blocks != 3 && t->min_blocks != 4) || t->tolerance < 0 ||
         t->tolerance > 1 || t->family_form < 0 || t->family_form > 1 ||
-        (t->inline_entries != 0 && t->inline_entries != 1 && t->inline_entries != 2)) {
+        (t->inline_entries != 0 && t->inline_entries != 1 && t->inline_entries != 2) ||
+        t->range_walk < 0 || t->range_walk > 1) {
         set_error("bgo_plan_set_tuning: chunk_sites 1024|2048, group_guides 32|64|128, "
                   "ctas_per_sm >= 0, split_families 0|1, min_blocks 3|4, tolerance 0|1, "
-                  "family_form 0|1, inline_entries 1|2");
+                  "family_form 0|1, inline_entries 1|2, range_walk 0|1");
         return BGO_ERR_ARG;
     }
     return BGO_OK;
@@ -710,7 +711,7 @@ extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
             q.fam_begin = fb;
             q.fam_end = fe;
             const int rc = launch_seed_kernel(q, sa, engine->sm_count, chunk, minb, t.tolerance,
-                                              t.inline_entries, t.ctas_per_sm, s);
+                                              t.inline_entries, t.range_walk, t.ctas_per_sm, s);
             if (rc == BGO_OK) engine->launches++;
             return rc;
         };

@@ -51,10 +51,12 @@ int launch_seed_t1(const ScanParams &p, const SeedArgs &sa, int sm_count, int ch
                    int min_blocks, int ctas_per_sm, cudaStream_t s);
 int launch_seed_t0i2(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
                      int min_blocks, int ctas_per_sm, cudaStream_t s);
+int launch_seed_t0walk(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
+                       int min_blocks, int ctas_per_sm, cudaStream_t s);
 
 int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
-                       int min_blocks, int tolerance, int inline_entries, int ctas_per_sm,
-                       cudaStream_t s) {
+                       int min_blocks, int tolerance, int inline_entries, int range_walk,
+                       int ctas_per_sm, cudaStream_t s) {
     if (chunk_sites != 1024 && chunk_sites != 2048) {
         set_error("segment index: chunk_sites must be 1024 or 2048");
         return BGO_ERR_ARG;
@@ -63,7 +65,9 @@ int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, in
         return launch_seed_t1(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
     if (inline_entries == 2)
         return launch_seed_t0i2(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
-    return launch_form<0, 1>(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
+    if (range_walk == 1)
+        return launch_seed_t0walk(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
+    return launch_form<0, 1, 0>(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
 }
 
 // PAM test program of a family: one test per constrained position (an N is

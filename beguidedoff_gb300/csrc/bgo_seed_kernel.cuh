@@ -1,7 +1,9 @@
 // Segment-indexed scan kernel (scan mode 2), included by the translation
 // units that instantiate its forms - tolerance 0 with one inline guide per
-// bucket (bgo_seed.cu), tolerance 0 with two (bgo_seed_i2.cu), tolerance 1
-// with two (bgo_seed_t1.cu) - so that they compile in parallel.  The algorithm is described at
+// bucket and the warp range queue (bgo_seed.cu) or the per-lane walk
+// (bgo_seed_walk.cu), tolerance 0 with two inline guides (bgo_seed_i2.cu),
+// tolerance 1 with two and the walk (bgo_seed_t1.cu) - so that they compile in
+// parallel.  The algorithm is described at
 // the top of bgo_seed.cu.
 #pragma once
 
@@ -76,7 +78,7 @@ __device__ __noinline__ void finish_candidate(const ScanParams &p, uint32_t m, i
           p.counter);
 }
 
-template <int K, int TOL, int INLINE, int CH, int MINB>
+template <int K, int TOL, int INLINE, int WALK, int CH, int MINB>
 __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParams p, SeedArgs sa) {
     using G = SegT<K, TOL>;
     constexpr int S = G::S;
@@ -275,8 +277,8 @@ __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParam
                 }
                 cand += T;
                 if (!__any_sync(0xFFFFFFFFu, R != 0u)) continue;
-                if constexpr (TOL == 1) {
-                    // tolerance-1 buckets rarely hold more than the inline two:
+                if constexpr (WALK == 1) {
+                    // buckets that rarely hold more than the inline guides:
                     // each lane walks its own few remaining entries
 #pragma unroll
                     for (int j = 0; j < S; ++j) {
@@ -338,56 +340,57 @@ __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParam
     if (t == 0 && sCand) atomicAdd(p.counter + 1, sCand);
 }
 
-template <int K, int TOL, int INLINE, int CH, int MINB>
+template <int K, int TOL, int INLINE, int WALK, int CH, int MINB>
 static int launch_k(const ScanParams &p, const SeedArgs &sa, int sm_count, int ctas_per_sm,
                     cudaStream_t s) {
     const size_t smem = seed_smem_bytes(sa, CH);
     static size_t configured = 0;
     if (smem > configured) {
-        BGO_CUDA(cudaFuncSetAttribute(scan_seed_kernel<K, TOL, INLINE, CH, MINB>,
+        BGO_CUDA(cudaFuncSetAttribute(scan_seed_kernel<K, TOL, INLINE, WALK, CH, MINB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
     }
     int per_sm = 0;
     BGO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, scan_seed_kernel<K, TOL, INLINE, CH, MINB>, kSeedThreads, smem));
+        &per_sm, scan_seed_kernel<K, TOL, INLINE, WALK, CH, MINB>, kSeedThreads, smem));
     if (per_sm < 1) per_sm = 1;
     if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
     const int64_t blocks_needed = (p.tiles_total + kSeedWarps - 1) / kSeedWarps;
     const int64_t grid = std::min<int64_t>(blocks_needed, (int64_t)sm_count * per_sm);
-    scan_seed_kernel<K, TOL, INLINE, CH, MINB><<<(unsigned)grid, kSeedThreads, smem, s>>>(p, sa);
+    scan_seed_kernel<K, TOL, INLINE, WALK, CH, MINB><<<(unsigned)grid, kSeedThreads, smem, s>>>(p, sa);
     BGO_CUDA(cudaGetLastError());
     return BGO_OK;
 }
 
-template <int TOL, int INLINE, int CH, int MINB>
+template <int TOL, int INLINE, int WALK, int CH, int MINB>
 static int launch_cm(const ScanParams &p, const SeedArgs &sa, int sm_count, int ctas_per_sm,
                      cudaStream_t s) {
     switch (p.max_mm) {
-        case 0: return launch_k<0, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 1: return launch_k<1, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 2: return launch_k<2, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 3: return launch_k<3, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 4: return launch_k<4, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 5: return launch_k<5, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 6: return launch_k<6, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
-        case 7: return launch_k<7, TOL, INLINE, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 0: return launch_k<0, TOL, INLINE, WALK, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 1: return launch_k<1, TOL, INLINE, WALK, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 2: return launch_k<2, TOL, INLINE, WALK, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 3: return launch_k<3, TOL, INLINE, WALK, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 4: return launch_k<4, TOL, INLINE, WALK, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 5: return launch_k<5, TOL, INLINE, WALK, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 6: return launch_k<6, TOL, INLINE, WALK, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
+        case 7: return launch_k<7, TOL, INLINE, WALK, CH, MINB>(p, sa, sm_count, ctas_per_sm, s);
         default:
             set_error("segment index: max_mismatches outside 0..7");
             return BGO_ERR_ARG;
     }
 }
 
-// All chunk lengths and occupancy targets for one (tolerance, inline) form.
-template <int TOL, int INLINE>
+// All chunk lengths and occupancy targets for one (tolerance, inline guides,
+// leftover walk) form.
+template <int TOL, int INLINE, int WALK>
 static int launch_form(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
                        int min_blocks, int ctas_per_sm, cudaStream_t s) {
     const bool c1k = chunk_sites == 1024;
     if (min_blocks == 4)
-        return c1k ? launch_cm<TOL, INLINE, 1024, 4>(p, sa, sm_count, ctas_per_sm, s)
-                   : launch_cm<TOL, INLINE, 2048, 4>(p, sa, sm_count, ctas_per_sm, s);
-    return c1k ? launch_cm<TOL, INLINE, 1024, 3>(p, sa, sm_count, ctas_per_sm, s)
-               : launch_cm<TOL, INLINE, 2048, 3>(p, sa, sm_count, ctas_per_sm, s);
+        return c1k ? launch_cm<TOL, INLINE, WALK, 1024, 4>(p, sa, sm_count, ctas_per_sm, s)
+                   : launch_cm<TOL, INLINE, WALK, 2048, 4>(p, sa, sm_count, ctas_per_sm, s);
+    return c1k ? launch_cm<TOL, INLINE, WALK, 1024, 3>(p, sa, sm_count, ctas_per_sm, s)
+               : launch_cm<TOL, INLINE, WALK, 2048, 3>(p, sa, sm_count, ctas_per_sm, s);
 }
 
 }  // namespace bgo

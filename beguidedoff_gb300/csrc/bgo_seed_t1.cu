@@ -9,7 +9,7 @@ namespace bgo {
 
 int launch_seed_t1(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
                    int min_blocks, int ctas_per_sm, cudaStream_t s) {
-    return launch_form<1, 2>(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
+    return launch_form<1, 2, 1>(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
 }
 
 }  // namespace bgo

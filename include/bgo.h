@@ -161,6 +161,9 @@ int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
  *   inline_entries  mode 2, tolerance 0: guides of each bucket compared inline
  *                 before the range queue, 1 or 2 (0 = 1); tolerance 1 always
  *                 compares 2
+ *   range_walk    mode 2, tolerance 0 with one inline guide: the rest of a
+ *                 bucket walked by its own lane (1) instead of spread over the
+ *                 warp (0); tolerance 1 always walks
  * Changing group_guides rebuilds the mask index at the next launch.  No
  * reference counterpart: the reference fixes 256 threads x 200 Mbp chunks.
  */
@@ -173,6 +176,8 @@ typedef struct bgo_tuning {
     int32_t tolerance;
     int32_t family_form;   /* per-family tuning only: 0 segment index, 1 compare every guide */
     int32_t inline_entries;
+    int32_t range_walk;
+    int32_t reserved[3];
 } bgo_tuning;
 int bgo_plan_set_tuning(bgo_plan *plan, const bgo_tuning *tuning);
 

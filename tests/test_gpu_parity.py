@@ -201,7 +201,8 @@ def test_indexed_modes_every_k_equal_oracle(k):
         tunings = [(0, 0, 0), (1024, 32, 0), (2048, 64, 2), (1024, 128, 1)]
         seed = [(0, 0, 0), (0, 0, 0, 1), (1024, 0, 0, 0, 4), (0, 0, 2, 1, 4), (1024, 0, 0, 0, 3),
                 (0, 0, 0, 0, 0, 1), (1024, 0, 0, 1, 4, 1), (2048, 0, 0, 1, 3, 1),
-                (0, 0, 0, 0, 0, 0, 2), (1024, 0, 0, 1, 4, 0, 2)]
+                (0, 0, 0, 0, 0, 0, 2), (1024, 0, 0, 1, 4, 0, 2), (0, 0, 0, 0, 0, 0, 0, 1),
+                (1024, 0, 0, 1, 4, 0, 0, 1)]
         for mode, tune in [(2, t) for t in seed] + [(3, t) for t in tunings]:
             plan.set_tuning(*tune)
             got = f._engine.scan(plan, f._strands, [0, 3], k, mode)
