@@ -89,6 +89,30 @@ def prepare_n_masks(genome: dict) -> Tuple[Optional[np.ndarray], Optional[np.nda
     return fwd, rc
 
 
+_ASCII = np.frombuffer(b"ACGT", dtype=np.uint8)
+
+
+def _decode_strings(seq: np.ndarray, pam: np.ndarray, plen: np.ndarray):
+    """Window and PAM strings of decoded 2-bit rows (object arrays of str)."""
+    n = seq.shape[0]
+    if n == 0:
+        return np.zeros(0, dtype=object), np.zeros(0, dtype=object)
+    s = np.ascontiguousarray(_ASCII[seq]).view("S20").ravel().astype("U20").astype(object)
+    pa = _ASCII[pam]
+    pa[np.arange(6)[None, :] >= plen[:, None]] = 0   # bytes strings end at the first NUL
+    p = np.ascontiguousarray(pa).view("S6").ravel().astype("U6").astype(object)
+    return s, p
+
+
+def _per_unique(values: np.ndarray, fn) -> np.ndarray:
+    """fn applied once per distinct value, spread back (an object array)."""
+    if values.size == 0:
+        return np.zeros(0, dtype=object)
+    uniq, inv = np.unique(values, return_inverse=True)
+    mapped = np.array([fn(v) for v in uniq.tolist()] + [None], dtype=object)[:-1]
+    return mapped[inv.ravel()]
+
+
 def window_cols(g) -> List[int]:
     """Guide positions of the edit window as Python indexes a 20-nt string:
     range(start - 1, end) below 20, negative indexes from the end
@@ -531,10 +555,9 @@ class beguidedoff:
             return Table()
         sizes = np.array([b.size for b in blocks], dtype=np.int64)
         idx = np.concatenate(blocks)
-        seq_s = ["".join(r) for r in _DECODE[seq[idx]]]
-        pam_s = ["".join(r[:k]) for r, k in zip(_DECODE[pam[idx]], plen[idx].tolist())]
-        mpos = [",".join(str(i + 1) for i in range(20) if (m >> i) & 1)
-                for m in mmask[idx].tolist()]
+        seq_s, pam_s = _decode_strings(seq[idx], pam[idx], plen[idx])
+        mpos = _per_unique(mmask[idx], lambda m: ",".join(str(i + 1) for i in range(20)
+                                                          if (m >> i) & 1))
         cols = {
             "guide_rna_sequence": np.array([plan_items[r][0] for r in row[idx].tolist()],
                                            dtype=object),
@@ -548,8 +571,7 @@ class beguidedoff:
             "ot_pam": np.array(pam_s, dtype=object),
             "n_mismatches": mm[idx].astype(np.int64),
             "mismatch_positions": np.array(mpos, dtype=object),
-            "score": np.array([round(float(v), 6) for v in score[idx].tolist()],
-                              dtype=np.float64),
+            "score": _per_unique(score[idx], lambda v: round(float(v), 6)).astype(np.float64),
             "n_offtargets_below_threshold": np.repeat(np.array(below, dtype=np.int64), sizes),
         }
         t = Table(cols, COLUMNS)
