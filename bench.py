@@ -374,7 +374,8 @@ def bench_ours(args, ws, rank, local):
         args.mode = f.last_choice.mode
     else:
         plan.set_tuning(args.chunk_sites, args.group_guides, args.ctas_per_sm,
-                        args.split_families, args.min_blocks, args.tolerance, args.inline_entries)
+                        args.split_families, args.min_blocks, args.tolerance, args.inline_entries,
+                        args.range_walk)
     if dense:
         editors = [DENSE_EDITORS[i % 3] for i in range(len(guides))]
     else:
@@ -743,6 +744,7 @@ def main():
     ap.add_argument("--tolerance", type=int, default=0, help="mode 2: key-region tolerance 0/1")
     ap.add_argument("--split-families", type=int, default=0, help="mode 2: one launch per family")
     ap.add_argument("--inline-entries", type=int, default=0, help="mode 2: 1 or 2 inline guides")
+    ap.add_argument("--range-walk", type=int, default=0, help="mode 2: per-lane walk of buckets")
     ap.add_argument("--genome-bp", type=int, default=3_100_000_000)
     ap.add_argument("--guides", type=int, default=100)
     ap.add_argument("--max-mm", type=int, default=4)
