@@ -37,6 +37,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "guide-site comparisons/s"
 UNIT = "cmp/s"
+# DRAM bytes (read + write) of one segment-index scan of the plain workload
+# at 300 Mbp, from ncu (profiles/scan_seed_kernel_ngg100_300mbp.md, capture 4);
+# traffic grows with the genome, so the line scales it to the run's length
+NCU_TRAFFIC_PLAIN = (300_000_000, 225.056e6 + 3.716864e6)
 
 
 def make_workload(genome_bp, n_guides, seed=2):
@@ -536,8 +540,14 @@ def bench_ours(args, ws, rank, local):
         if args.mode in (2, 3):
             # the segment index makes the compares sub-linear in guides: the
             # floor of a full scan is streaming both strands' planes once
+            traffic = None
+            if args.config == "plain" and not getattr(args, "families", ""):
+                bp, nbytes = NCU_TRAFFIC_PLAIN
+                traffic = nbytes * total / bp
             roof = {"bound": "hbm", "unit": "GB/s", "achieved": hbm_achieved, "peak": hbm_peak,
-                    "frac": hbm_achieved / hbm_peak, "traffic": None,
+                    "frac": hbm_achieved / hbm_peak, "traffic": traffic,
+                    "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at "
+                                      "300 Mbp, scaled by genome length" if traffic else None,
                     "bytes_per_step": plane_bytes,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                     "int_popc": popc}
