@@ -41,6 +41,12 @@ UNIT = "cmp/s"
 # at 300 Mbp, from ncu (profiles/scan_seed_kernel_ngg100_300mbp.md, capture 4);
 # traffic grows with the genome, so the line scales it to the run's length
 NCU_TRAFFIC_PLAIN = (300_000_000, 225.056e6 + 3.716864e6)
+# the same capture's integer-pipe figures: the kernel is issue-bound, so these
+# are its roofline in the north-star's integer-ALU sense
+NCU_INT_PLAIN = {"issue_active_frac": 0.683, "alu_pipe_active_frac": 0.615,
+                 "warps_active_frac": 0.338,
+                 "source": "ncu smsp__issue_active, sm__pipe_alu_cycles_active, "
+                           "sm__warps_active (pct of peak, active cycles) at 300 Mbp"}
 
 
 def make_workload(genome_bp, n_guides, seed=2):
@@ -540,17 +546,18 @@ def bench_ours(args, ws, rank, local):
         if args.mode in (2, 3):
             # the segment index makes the compares sub-linear in guides: the
             # floor of a full scan is streaming both strands' planes once
-            traffic = None
+            traffic, int_pipes = None, None
             if args.config == "plain" and not getattr(args, "families", ""):
                 bp, nbytes = NCU_TRAFFIC_PLAIN
                 traffic = nbytes * total / bp
+                int_pipes = NCU_INT_PLAIN
             roof = {"bound": "hbm", "unit": "GB/s", "achieved": hbm_achieved, "peak": hbm_peak,
                     "frac": hbm_achieved / hbm_peak, "traffic": traffic,
                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at "
                                       "300 Mbp, scaled by genome length" if traffic else None,
                     "bytes_per_step": plane_bytes,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-                    "int_popc": popc}
+                    "int_popc": popc, "int_pipes_ncu": int_pipes}
         else:
             roof = {"bound": "int", "unit": "Gop/s", "achieved": achieved, "peak": popc_peak,
                     "frac": achieved / popc_peak, "traffic": None,
