@@ -182,7 +182,7 @@ def test_autotuned_scan_equals_oracle():
         f.close()
 
 
-@pytest.mark.parametrize("k", [0, 1, 2, 3, 6, 7])
+@pytest.mark.parametrize("k", [0, 1, 2, 3, 4, 5, 6, 7])
 def test_indexed_modes_every_k_equal_oracle(k):
     """Segment index (mode 2) and segment masks (mode 3) at every segment
     layout they compile, against the oracle; mode 3 also at each tuning."""
@@ -306,6 +306,47 @@ def test_device_epilogue_ties_and_chromosome_order():
                 got = table_rows(f.search(guides=guides, verbose=False, **kw))
                 ok, why = rows_equal(got, exp)
                 assert ok, f"n_top {n_top} {kw}: {why}"
+    finally:
+        f.close()
+
+
+def test_five_prime_pams_every_form_equals_oracle():
+    """5'-PAM rows (window after the PAM) mixed with 3' rows, through every
+    scan form and the indexed forms' tunings, against the C oracle."""
+    genome, rng = _random_genome(91, [500_000, 300_001])
+    k = 4
+    seqs, pams, p3 = [], [], []
+    for i in range(40):
+        seqs.append("".join(rng.choice(list("ACGT"), 20)))
+        pams.append(["TTTV", "NGG", "TTN", "NNGRRT"][i % 4])
+        p3.append(0 if i % 2 == 0 else 1)
+    gv = np.array([O.encode_guide(s_) for s_ in seqs], dtype=np.uint64)
+    pm = np.zeros((len(seqs), 6), dtype=np.uint8)
+    for i, pam in enumerate(pams):
+        for j, ch in enumerate(pam):
+            pm[i, j] = IUPAC[ch]
+    pl = np.array([len(p_) for p_ in pams], dtype=np.uint8)
+    p3 = np.array(p3, dtype=np.uint8)
+    fwd, rc = O.prepare_n_masks(genome)
+    exp = []
+    for slot, (arr, nm, ne) in enumerate(((genome["genome_forward"], fwd, 0),
+                                          (genome["genome_rc"], rc, 3))):
+        _, keys = O.scan_strand(arr, genome["total_bp"], nm, gv, pm, pl, p3, k, ne)
+        g_, pos, mm = O.split_keys(keys)
+        exp.append((g_.astype(np.uint64) << np.uint64(39)) | (np.uint64(slot) << np.uint64(38))
+                   | (pos.astype(np.uint64) << np.uint64(6)) | mm.astype(np.uint64))
+    exp = np.sort(np.concatenate(exp))
+    assert exp.size > 0
+    f = beguidedoff(None, max_mismatches=k, genome_data=genome)
+    try:
+        plan = _native.Plan(f._engine, gv, pm, pl, p3)
+        forms = [(0, ()), (1, ()), (2, ()), (2, (0, 0, 0, 1)), (2, (0, 0, 0, 0, 0, 1)),
+                 (2, (1024, 0, 0, 1, 4, 0, 2)), (2, (0, 0, 0, 0, 0, 0, 0, 1)), (3, (2048, 64))]
+        for mode, tune in forms:
+            plan.set_tuning(*tune)
+            got = f._engine.scan(plan, f._strands, [0, 3], k, mode)
+            assert np.array_equal(got, exp), (mode, tune)
+        plan.close()
     finally:
         f.close()
 
