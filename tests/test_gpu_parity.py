@@ -351,6 +351,37 @@ def test_five_prime_pams_every_form_equals_oracle():
         f.close()
 
 
+def test_forward_only_genome_and_large_k():
+    """A genome without genome_rc (one strand) through the device path, and
+    max_mismatches 8-9 where the indexed forms fall back to every guide."""
+    genome, rng = _random_genome(93, [300_000, 180_001])
+    seqs = ["".join(rng.choice(list("ACGT"), 20)) for _ in range(6)]
+    for s_ in seqs:
+        _plant(genome, rng, s_, "NGG", 3, 4)
+    fwd_only = {k_: v for k_, v in genome.items() if k_ != "genome_rc"}
+    guides = [GuideInput(f"g{i}", s_, "NGG", "3prime", 4, 8, "ABE") for i, s_ in enumerate(seqs)]
+    host = beguidedoff.host_only(fwd_only, 4)
+    host._scan = lambda sq, pm: oracle_keys(fwd_only, sq, pm, 4)
+    f = beguidedoff(None, max_mismatches=4, genome_data=fwd_only)
+    try:
+        for kw in ({}, {"return_all": True, "count_score_threshold": 3.0}):
+            ok, why = rows_equal(table_rows(f.search(guides=guides, verbose=False, **kw)),
+                                 table_rows(host.search(guides=guides, verbose=False, **kw)))
+            assert ok, (kw, why)
+    finally:
+        f.close()
+    f = beguidedoff(None, max_mismatches=8, genome_data=genome)
+    try:
+        for k in (8, 9):
+            exp = oracle_keys(genome, seqs[:2], ["NGG"] * 2, k)
+            plan = f._plan(seqs[:2], ["NGG"] * 2)
+            for mode in (2, 3):
+                assert np.array_equal(f._engine.scan(plan, f._strands, [0, 3], k, mode), exp)
+            plan.close()
+    finally:
+        f.close()
+
+
 def test_graph_replay_equals_launch():
     """A captured scan (bgo_graph_create / bgo_graph_launch) returns the same
     keys as ordinary launches, on every replay, for the plain and indexed forms."""
