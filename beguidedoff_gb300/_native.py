@@ -487,12 +487,28 @@ class Engine:
               "bgo_engine_transfer")
         return {"h2d": a.value, "d2h": b.value}
 
+    # input rows per bgo_epilogue_run call: its scratch holds a 16 KB rank
+    # histogram per row, so larger row sets run in chunks (rows are independent)
+    EPILOGUE_ROWS_PER_CALL = 131072
+
     def epilogue(self, plan, strands, inputs, chrom_offsets, chrom_lengths, chrom_rank,
                  rank_table, n_top, stream=None):
         """Device epilogue of the last scan (bgo_epilogue_run + fetch):
         (below[n_inputs], group_counts[n_plan_rows, 2], row_counts[n_inputs],
         records grouped by input row)."""
         inputs = np.ascontiguousarray(inputs, dtype=INPUT_ROW_DTYPE)
+        step = self.EPILOGUE_ROWS_PER_CALL
+        if inputs.size > step:
+            parts = [self.epilogue(plan, strands, inputs[i:i + step], chrom_offsets,
+                                   chrom_lengths, chrom_rank, rank_table, n_top, stream)
+                     for i in range(0, inputs.size, step)]
+            recs = []
+            for i, p in zip(range(0, inputs.size, step), parts):
+                r = p[3].copy()
+                r["input_row"] += i
+                recs.append(r)
+            return (np.concatenate([p[0] for p in parts]), parts[0][1],
+                    np.concatenate([p[2] for p in parts]), np.concatenate(recs))
         offs = np.ascontiguousarray(chrom_offsets, dtype=np.int64)
         lens = np.ascontiguousarray(chrom_lengths, dtype=np.int64)
         crank = np.ascontiguousarray(chrom_rank, dtype=np.int32)

@@ -382,6 +382,26 @@ def test_forward_only_genome_and_large_k():
         f.close()
 
 
+def test_epilogue_row_chunks_equal_one_call(monkeypatch):
+    """Input rows split over several bgo_epilogue_run calls give the records,
+    counts and tables of one call."""
+    genome, rng = _random_genome(95, [400_000, 250_001])
+    seqs = ["".join(rng.choice(list("ACGT"), 20)) for _ in range(12)]
+    for s_ in seqs:
+        _plant(genome, rng, s_, "NGG", 6, 4)
+    guides = [GuideInput(f"g{i % 5}", s_, "NGG", "3prime", 1 + i % 5, 12, "ABE" if i % 2 else "CBE")
+              for i, s_ in enumerate(seqs)]
+    f = beguidedoff(None, max_mismatches=4, genome_data=genome)
+    try:
+        one = table_rows(f.search(guides=guides, verbose=False, count_score_threshold=4.0))
+        monkeypatch.setattr(_native.Engine, "EPILOGUE_ROWS_PER_CALL", 5)
+        many = table_rows(f.search(guides=guides, verbose=False, count_score_threshold=4.0))
+        ok, why = rows_equal(many, one)
+        assert ok and len(one) > 0, why
+    finally:
+        f.close()
+
+
 def test_graph_replay_equals_launch():
     """A captured scan (bgo_graph_create / bgo_graph_launch) returns the same
     keys as ordinary launches, on every replay, for the plain and indexed forms."""
