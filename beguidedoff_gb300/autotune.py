@@ -14,8 +14,9 @@ a power of two.
 Candidate parameters: scan mode; tile length (positions per warp chunk,
 ``chunk_sites``); guides per mask group (``group_guides``, mode 3); one
 launch per PAM family (``split_families``, mode 2); CTAs per SM the kernel is
-compiled for (``min_blocks``: 3 with up to 80 registers, or 4 with up to 64,
-mode 2); mismatches tolerated per key region (``tolerance``: 0 with K + 1
+compiled for (``min_blocks``: 3 or 4 CTAs of 256 threads with up to 80 or 64
+registers, or 1 CTA of 768 threads whose 24 warps share one copy of the
+index, mode 2); mismatches tolerated per key region (``tolerance``: 0 with K + 1
 regions, or 1 with K / 2 + 1 regions and substitution-expanded buckets,
 mode 2).
 """
@@ -39,6 +40,8 @@ CANDIDATES: Tuple[Tuple[str, int, Tuple[int, ...]], ...] = (
     ("segment-index/t1/1024", 2, (1024, 0, 0, 0, 0, 1, 0)),
     ("segment-index/t1/per-family", 2, (0, 0, 0, 1, 0, 1, 0)),
     ("segment-index/t1/per-family/1024", 2, (1024, 0, 0, 1, 0, 1, 0)),
+    ("segment-index/t1/cta768", 2, (0, 0, 0, 0, 1, 1, 0)),
+    ("segment-index/walk/cta768", 2, (0, 0, 0, 0, 1, 0, 0, 1)),
     ("segment-masks/2048x128", 3, (2048, 128, 0, 0, 0, 0, 0)),
 )
 TUNING_FIELDS = ("chunk_sites", "group_guides", "ctas_per_sm", "split_families", "min_blocks",
@@ -55,6 +58,9 @@ FAMILY_CANDIDATES = (
     ("index/t1", 0, 0, 0, 1, 0, 0),
     ("index/t1/1024", 0, 1024, 0, 1, 0, 0),
     ("index/t1/1024/occ4", 0, 1024, 4, 1, 0, 0),
+    ("index/walk/cta768", 0, 0, 1, 0, 0, 1),
+    ("index/t1/cta768", 0, 0, 1, 1, 0, 0),
+    ("index/t1/1024/cta768", 0, 1024, 1, 1, 0, 0),
 )
 PER_FAMILY_TUNING = (0, 0, 0, 1, 0, 0, 0, 0)
 INDEXED_MAX_K = 7

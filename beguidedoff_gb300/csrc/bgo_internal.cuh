@@ -228,7 +228,9 @@ bool build_seed_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, 
                       const std::vector<int> &tols,
                       std::vector<SeedFam> &out_fams, std::vector<uint32_t> &offsets,
                       std::vector<uint2> &entries, std::vector<uint16_t> &entry_idx);
-size_t seed_smem_bytes(const SeedArgs &sa, int chunk_sites);
+size_t seed_smem_bytes(const SeedArgs &sa, int chunk_sites, int warps, bool walk);
+// dynamic shared memory of the segment-index kernel form a tuning selects
+size_t seed_tuning_smem(const SeedArgs &sa, const bgo_tuning &t);
 int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
                        int min_blocks, int tolerance, int inline_entries, int range_walk,
                        int ctas_per_sm, cudaStream_t s);

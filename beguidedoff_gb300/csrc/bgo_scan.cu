@@ -403,12 +403,13 @@ static int check_tuning(const bgo_plan *pl, const bgo_tuning *t) {
         (t->group_guides != 0 && t->group_guides != 32 && t->group_guides != 64 &&
          t->group_guides != 128) ||
         t->ctas_per_sm < 0 || t->split_families < 0 || t->split_families > 1 ||
-        (t->min_blocks != 0 && t->min_blocks != 3 && t->min_blocks != 4) || t->tolerance < 0 ||
+        (t->min_blocks != 0 && t->min_blocks != 1 && t->min_blocks != 3 && t->min_blocks != 4) ||
+        t->tolerance < 0 ||
         t->tolerance > 1 || t->family_form < 0 || t->family_form > 1 ||
         (t->inline_entries != 0 && t->inline_entries != 1 && t->inline_entries != 2) ||
         t->range_walk < 0 || t->range_walk > 1) {
         set_error("bgo_plan_set_tuning: chunk_sites 1024|2048, group_guides 32|64|128, "
-                  "ctas_per_sm >= 0, split_families 0|1, min_blocks 3|4, tolerance 0|1, "
+                  "ctas_per_sm >= 0, split_families 0|1, min_blocks 1|3|4, tolerance 0|1, "
                   "family_form 0|1, inline_entries 1|2, range_walk 0|1");
         return BGO_ERR_ARG;
     }
@@ -480,21 +481,19 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
     if (split)
         for (int f = 0; f < pl->n_families; ++f) tols[(size_t)f] = family_tuning(pl, f).tolerance;
     const size_t limit = 220 * 1024;
-    auto chunk_of = [](const bgo_tuning &t) { return t.chunk_sites ? t.chunk_sites : 2048; };
     auto applies = [&]() -> int {
         if (!pl->seed_ok) return 0;
         if (split) {
             for (int f = 0; f < pl->n_families; ++f) {
                 const bgo_tuning &t = family_tuning(pl, f);
-                if (t.family_form == 0 &&
-                    seed_smem_bytes(pl->seed_fam[(size_t)f], chunk_of(t)) > limit)
+                if (t.family_form == 0 && seed_tuning_smem(pl->seed_fam[(size_t)f], t) > limit)
                     return 0;
             }
             return 1;
         }
         for (int v : tols)
             if (v != tols[0]) return 0;  // one launch needs one tolerance
-        return seed_smem_bytes(pl->seed, chunk_of(pl->tuning)) <= limit ? 1 : 0;
+        return seed_tuning_smem(pl->seed, pl->tuning) <= limit ? 1 : 0;
     };
     if (pl->seed_k == K && pl->seed_tols == tols) return applies();
     if (pl->d_seed || pl->d_seed_fam) {

@@ -39,12 +39,24 @@
 
 namespace bgo {
 
-size_t seed_smem_bytes(const SeedArgs &sa, int chunk_sites) {
+size_t seed_smem_bytes(const SeedArgs &sa, int chunk_sites, int warps, bool walk) {
     size_t b = sizeof(SeedFam) * sa.n_fams + sizeof(uint2) * sa.n_lists +
                sizeof(uint32_t) * sa.n_offsets + sizeof(uint16_t) * sa.n_lists;
     b = (b + 15) / 16 * 16;
-    const size_t slice = chunk_sites == 1024 ? SeedChunk<1024>::kSlice : SeedChunk<2048>::kSlice;
-    return b + kSeedWarps * slice;
+    const size_t slice = chunk_sites == 1024
+                             ? (walk ? SeedChunk<1024, 1>::kSlice : SeedChunk<1024, 0>::kSlice)
+                             : (walk ? SeedChunk<2048, 1>::kSlice : SeedChunk<2048, 0>::kSlice);
+    return b + (size_t)warps * slice;
+}
+
+// The kernel form a tuning selects walks its leftover guides per lane for
+// tolerance 1 (always), and for tolerance 0 with range_walk unless two guides
+// per bucket are compared inline; launch_seed_kernel dispatches the same way.
+size_t seed_tuning_smem(const SeedArgs &sa, const bgo_tuning &t) {
+    const int chunk = t.chunk_sites ? t.chunk_sites : 2048;
+    const int warps = t.min_blocks == 1 ? SeedCta<1>::kWarps : SeedCta<3>::kWarps;
+    const bool walk = t.tolerance == 1 || (t.inline_entries != 2 && t.range_walk == 1);
+    return seed_smem_bytes(sa, chunk, warps, walk);
 }
 
 int launch_seed_t1(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,

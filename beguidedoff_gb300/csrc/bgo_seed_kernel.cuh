@@ -21,9 +21,10 @@ constexpr int kSeedWarps = kSeedThreads / 32;
 constexpr int kQueueCap = 32 * (kSeedMaxK + 1);  // bucket ranges per round
 
 // Per-warp shared-memory slice for chunks of CH positions: two chunk buffers
-// (H, L, N planes), the compacted list, the round's position records and the
-// bucket-range queue (word + count).
-template <int CH>
+// (H, L, N planes), the compacted list, and, unless the lanes walk their own
+// leftover guides (WALK), the round's position records and the bucket-range
+// queue (word + count).
+template <int CH, int WALK>
 struct SeedChunk {
     static constexpr int kRows = CH / 1024;      // 32-position words per lane
     static constexpr int kWords = CH / 32 + 4;   // + halo, a multiple of 4 words
@@ -33,7 +34,8 @@ struct SeedChunk {
     static constexpr size_t kRecOff = (kListOff + CH * sizeof(uint16_t) + 15) / 16 * 16;
     static constexpr size_t kQueueOff = kRecOff + 32 * sizeof(uint4);
     static constexpr size_t kCountOff = kQueueOff + kQueueCap * sizeof(uint32_t);
-    static constexpr size_t kSlice = (kCountOff + kQueueCap * sizeof(uint16_t) + 15) / 16 * 16;
+    static constexpr size_t kSlice =
+        WALK ? kRecOff : (kCountOff + kQueueCap * sizeof(uint16_t) + 15) / 16 * 16;
     static_assert(kWords % 4 == 0, "chunk copies are whole 16-byte vectors");
     static_assert(kBuf % 16 == 0, "chunk buffers stay 16-byte aligned");
 };
@@ -78,11 +80,22 @@ __device__ __noinline__ void finish_candidate(const ScanParams &p, uint32_t m, i
           p.counter);
 }
 
+// CTAs are 256 threads (MINB = 3 or 4 per SM), or one 768-thread CTA per SM
+// (MINB = 1) so that 24 warps share a large index.
+template <int MINB>
+struct SeedCta {
+    static constexpr int kThreads = MINB == 1 ? 768 : kSeedThreads;
+    static constexpr int kWarps = kThreads / 32;
+};
+
 template <int K, int TOL, int INLINE, int WALK, int CH, int MINB>
-__global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParams p, SeedArgs sa) {
+__global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
+    scan_seed_kernel(ScanParams p, SeedArgs sa) {
+    constexpr int THREADS = SeedCta<MINB>::kThreads;
+    constexpr int WARPS = SeedCta<MINB>::kWarps;
     using G = SegT<K, TOL>;
     constexpr int S = G::S;
-    using C = SeedChunk<CH>;
+    using C = SeedChunk<CH, WALK>;
     extern __shared__ __align__(16) unsigned char smem[];
     SeedFam *sFam = reinterpret_cast<SeedFam *>(smem);
     uint2 *sEnt = reinterpret_cast<uint2 *>(sFam + sa.n_fams);
@@ -102,18 +115,18 @@ __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParam
     uint32_t *wQ = reinterpret_cast<uint32_t *>(slice + C::kQueueOff);
     uint16_t *wCnt = reinterpret_cast<uint16_t *>(slice + C::kCountOff);
 
-    for (int i = t; i < sa.n_fams; i += kSeedThreads) sFam[i] = sa.fams[i];
-    for (int i = t; i < sa.n_lists; i += kSeedThreads) {
+    for (int i = t; i < sa.n_fams; i += THREADS) sFam[i] = sa.fams[i];
+    for (int i = t; i < sa.n_lists; i += THREADS) {
         sEnt[i] = sa.entries[i];
         sIdx[i] = sa.entry_idx[i];
     }
-    for (int i = t; i < sa.n_offsets; i += kSeedThreads) sOff[i] = sa.offsets[i];
+    for (int i = t; i < sa.n_offsets; i += THREADS) sOff[i] = sa.offsets[i];
     if (t == 0) sCand = 0;
     __syncthreads();
 
     const int64_t chunks0 = p.strand[0].n_tiles;
     const int64_t n_chunks = p.tiles_total;
-    const int64_t stride = (int64_t)gridDim.x * kSeedWarps;
+    const int64_t stride = (int64_t)gridDim.x * WARPS;
     // Chunk c's words [c*CH/32, c*CH/32 + kWords) of the three planes, copied
     // into buffer b as 16-byte vectors (the planes are padded so that the copy
     // never leaves them, and zero beyond total_bp).
@@ -129,7 +142,7 @@ __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParam
         }
     };
     uint32_t cand = 0;
-    const int64_t c_first = (int64_t)blockIdx.x * kSeedWarps + warp;
+    const int64_t c_first = (int64_t)blockIdx.x * WARPS + warp;
     if (c_first < n_chunks) issue(c_first, 0);
     cp_async_commit();
     int buf = 0;
@@ -343,7 +356,7 @@ __global__ void __launch_bounds__(kSeedThreads, MINB) scan_seed_kernel(ScanParam
 template <int K, int TOL, int INLINE, int WALK, int CH, int MINB>
 static int launch_k(const ScanParams &p, const SeedArgs &sa, int sm_count, int ctas_per_sm,
                     cudaStream_t s) {
-    const size_t smem = seed_smem_bytes(sa, CH);
+    const size_t smem = seed_smem_bytes(sa, CH, SeedCta<MINB>::kWarps, WALK == 1);
     static size_t configured = 0;
     if (smem > configured) {
         BGO_CUDA(cudaFuncSetAttribute(scan_seed_kernel<K, TOL, INLINE, WALK, CH, MINB>,
@@ -352,12 +365,15 @@ static int launch_k(const ScanParams &p, const SeedArgs &sa, int sm_count, int c
     }
     int per_sm = 0;
     BGO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, scan_seed_kernel<K, TOL, INLINE, WALK, CH, MINB>, kSeedThreads, smem));
+        &per_sm, scan_seed_kernel<K, TOL, INLINE, WALK, CH, MINB>, SeedCta<MINB>::kThreads,
+        smem));
     if (per_sm < 1) per_sm = 1;
     if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
-    const int64_t blocks_needed = (p.tiles_total + kSeedWarps - 1) / kSeedWarps;
+    constexpr int WARPS = SeedCta<MINB>::kWarps;
+    const int64_t blocks_needed = (p.tiles_total + WARPS - 1) / WARPS;
     const int64_t grid = std::min<int64_t>(blocks_needed, (int64_t)sm_count * per_sm);
-    scan_seed_kernel<K, TOL, INLINE, WALK, CH, MINB><<<(unsigned)grid, kSeedThreads, smem, s>>>(p, sa);
+    scan_seed_kernel<K, TOL, INLINE, WALK, CH, MINB>
+        <<<(unsigned)grid, SeedCta<MINB>::kThreads, smem, s>>>(p, sa);
     BGO_CUDA(cudaGetLastError());
     return BGO_OK;
 }
@@ -389,6 +405,9 @@ static int launch_form(const ScanParams &p, const SeedArgs &sa, int sm_count, in
     if (min_blocks == 4)
         return c1k ? launch_cm<TOL, INLINE, WALK, 1024, 4>(p, sa, sm_count, ctas_per_sm, s)
                    : launch_cm<TOL, INLINE, WALK, 2048, 4>(p, sa, sm_count, ctas_per_sm, s);
+    if (min_blocks == 1)
+        return c1k ? launch_cm<TOL, INLINE, WALK, 1024, 1>(p, sa, sm_count, ctas_per_sm, s)
+                   : launch_cm<TOL, INLINE, WALK, 2048, 1>(p, sa, sm_count, ctas_per_sm, s);
     return c1k ? launch_cm<TOL, INLINE, WALK, 1024, 3>(p, sa, sm_count, ctas_per_sm, s)
                : launch_cm<TOL, INLINE, WALK, 2048, 3>(p, sa, sm_count, ctas_per_sm, s);
 }
