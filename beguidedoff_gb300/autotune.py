@@ -41,7 +41,9 @@ CANDIDATES: Tuple[Tuple[str, int, Tuple[int, ...]], ...] = (
     ("segment-index/t1/per-family", 2, (0, 0, 0, 1, 0, 1, 0)),
     ("segment-index/t1/per-family/1024", 2, (1024, 0, 0, 1, 0, 1, 0)),
     ("segment-index/t1/cta768", 2, (0, 0, 0, 0, 1, 1, 0)),
+    ("segment-index/t1/1024/cta768", 2, (1024, 0, 0, 0, 1, 1, 0)),
     ("segment-index/walk/cta768", 2, (0, 0, 0, 0, 1, 0, 0, 1)),
+    ("segment-index/walk/1024/cta768", 2, (1024, 0, 0, 0, 1, 0, 0, 1)),
     ("segment-masks/2048x128", 3, (2048, 128, 0, 0, 0, 0, 0)),
 )
 TUNING_FIELDS = ("chunk_sites", "group_guides", "ctas_per_sm", "split_families", "min_blocks",

@@ -475,25 +475,39 @@ static const bgo_tuning &family_tuning(const bgo_plan *pl, int f) {
     return pl->fam_tuning.empty() ? pl->tuning : pl->fam_tuning[(size_t)f];
 }
 
+// The tuning a segment-index launch over index `sa` runs with: the requested
+// one when the index and the warps' chunk slices fit in shared memory, else
+// the same tolerance and form with 1,024-position chunks, then with 8 warps per
+// CTA, then both.  False when none fits (the family, or the single launch,
+// compares every guide instead).
+static bool fitted_seed_tuning(const SeedArgs &sa, const bgo_tuning &t, bgo_tuning &out) {
+    const size_t limit = 220 * 1024;
+    bgo_tuning c = t;
+    for (int step = 0; step < 4; ++step) {
+        c.chunk_sites = (step & 1) ? 1024 : t.chunk_sites;
+        c.min_blocks = (step & 2) && t.min_blocks == 1 ? 3 : t.min_blocks;
+        if (seed_tuning_smem(sa, c) <= limit) {
+            out = c;
+            return true;
+        }
+    }
+    return false;
+}
+
 static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s) {
     const bool split = pl->tuning.split_families && pl->n_families > 1;
     std::vector<int> tols((size_t)pl->n_families, pl->tuning.tolerance);
     if (split)
         for (int f = 0; f < pl->n_families; ++f) tols[(size_t)f] = family_tuning(pl, f).tolerance;
-    const size_t limit = 220 * 1024;
+    // split launches: a family whose index does not fit in any form compares
+    // every guide on its own
     auto applies = [&]() -> int {
         if (!pl->seed_ok) return 0;
-        if (split) {
-            for (int f = 0; f < pl->n_families; ++f) {
-                const bgo_tuning &t = family_tuning(pl, f);
-                if (t.family_form == 0 && seed_tuning_smem(pl->seed_fam[(size_t)f], t) > limit)
-                    return 0;
-            }
-            return 1;
-        }
+        if (split) return 1;
         for (int v : tols)
             if (v != tols[0]) return 0;  // one launch needs one tolerance
-        return seed_tuning_smem(pl->seed, pl->tuning) <= limit ? 1 : 0;
+        bgo_tuning fit;
+        return fitted_seed_tuning(pl->seed, pl->tuning, fit) ? 1 : 0;
     };
     if (pl->seed_k == K && pl->seed_tols == tols) return applies();
     if (pl->d_seed || pl->d_seed_fam) {
@@ -730,14 +744,18 @@ extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
         };
         if (plan->tuning.split_families && plan->n_families > 1) {
             for (int f = 0; f < plan->n_families; ++f) {
-                const bgo_tuning &t = family_tuning(plan, f);
-                const int rc = t.family_form == 1
-                                   ? every_guide_launch(f, f + 1)
-                                   : seed_launch(f, f + 1, plan->seed_fam[(size_t)f], t);
+                const SeedArgs &sa = plan->seed_fam[(size_t)f];
+                bgo_tuning fit;
+                const int rc = family_tuning(plan, f).family_form == 0 &&
+                                       fitted_seed_tuning(sa, family_tuning(plan, f), fit)
+                                   ? seed_launch(f, f + 1, sa, fit)
+                                   : every_guide_launch(f, f + 1);
                 if (rc != BGO_OK) return rc;
             }
         } else {
-            const int rc = seed_launch(0, plan->n_families, plan->seed, plan->tuning);
+            bgo_tuning fit;
+            fitted_seed_tuning(plan->seed, plan->tuning, fit);  // applies() checked it fits
+            const int rc = seed_launch(0, plan->n_families, plan->seed, fit);
             if (rc != BGO_OK) return rc;
         }
     } else {

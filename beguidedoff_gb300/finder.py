@@ -333,10 +333,12 @@ class beguidedoff:
                 eng.reserve(n)
                 eng.launch(plan, self._strands, ne, max_mismatches, mode, stream)
             t2 = time.perf_counter()
-            self.last_batch = {"hits": n, "plan_rows": len(plan_items), "mode": mode,
-                               "plan_s": t1 - t0, "scan_s": t2 - t1}
+            # this batch's own record (batches of several serving slots run
+            # concurrently; last_batch only ever receives a finished record)
+            stats = {"hits": n, "plan_rows": len(plan_items), "mode": mode,
+                     "plan_s": t1 - t0, "scan_s": t2 - t1}
             if info is not None:
-                info.update(self.last_batch)
+                info.update(stats)
             parts, owners, spans, errs = [], [], [], []
             n_rows = 0
             for r in reqs:
@@ -401,10 +403,11 @@ class beguidedoff:
                                               r["count_score_threshold"], log, precomputed=pre))
                 except Exception as exc:  # reported to that request only
                     out.append(exc)
-            self.last_batch["epilogue_s"] = (t3 - t2) if parts else 0.0
-            self.last_batch["assemble_s"] = time.perf_counter() - (t3 if parts else t2)
+            stats["epilogue_s"] = (t3 - t2) if parts else 0.0
+            stats["assemble_s"] = time.perf_counter() - (t3 if parts else t2)
             if info is not None:
-                info.update(self.last_batch)
+                info.update(stats)
+            self.last_batch = stats
             return out
         finally:
             plan.close()

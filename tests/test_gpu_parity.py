@@ -224,6 +224,43 @@ def test_indexed_modes_every_k_equal_oracle(k):
         f.close()
 
 
+def test_index_forms_that_outgrow_shared_memory_equal_oracle():
+    """Families large enough that the requested segment-index form (768-thread
+    CTAs, 2,048-position chunks) does not fit in shared memory run in the next
+    form that fits (1,024-position chunks, then 8 warps) or compare every guide;
+    the keys stay the oracle's in one launch and in per-family launches."""
+    genome, rng = _random_genome(91, [300_000, 120_001])
+    seqs, pams = [], []
+    # at K = 5 with tolerance 1: NNGRRT fits 768 threads with 1,024-position
+    # chunks, NG 8 warps with 2,048, NRN 8 warps with 1,024, NGG no form
+    for fam, n in (("NRN", 250), ("NG", 200), ("NGG", 1500), ("NNGRRT", 150)):
+        for i in range(n):
+            s = "".join(rng.choice(list("ACGT"), 20))
+            if i % 50 == 0:
+                _plant(genome, rng, s, fam, 3, 5)
+            seqs.append(s)
+            pams.append(fam)
+    exp = oracle_keys(genome, seqs, pams, 5)
+    assert exp.size > 100
+    f = beguidedoff(None, max_mismatches=5, genome_data=genome)
+    try:
+        plan = f._plan(seqs, pams)
+        for tune in [(0, 0, 0, 0, 1, 1), (0, 0, 0, 0, 1, 0, 0, 1), (0, 0, 0, 0, 1, 0, 2)]:
+            plan.set_tuning(*tune)
+            got = f._engine.scan(plan, f._strands, [0, 3], 5, 2)
+            assert np.array_equal(got, exp), tune
+        for fam_tune in [dict(tolerance=1, min_blocks=1), dict(min_blocks=1, range_walk=1),
+                         dict(min_blocks=1, inline_entries=2), dict(tolerance=1)]:
+            plan.set_tuning(0, 0, 0, 1)
+            for fi in range(plan.families().max() + 1):
+                plan.set_family_tuning(fi, **fam_tune)
+            got = f._engine.scan(plan, f._strands, [0, 3], 5, 2)
+            assert np.array_equal(got, exp), fam_tune
+        plan.close()
+    finally:
+        f.close()
+
+
 @pytest.mark.parametrize("seed", [31, 32])
 def test_device_epilogue_tables_equal_host_assembly(seed):
     """Device epilogue (exact score ranks, on-target exclusion, editable
