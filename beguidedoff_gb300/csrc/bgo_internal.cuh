@@ -154,6 +154,17 @@ inline int64_t seed_tiles_for(int64_t total_bp, int chunk_sites = kSeedChunkSite
 void set_error(const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
 
+// Plans and their indexes take device memory from one stream-ordered pool per
+// device, so creating and destroying them never synchronises the device (a
+// cudaFree waits for every stream, e.g. another serving slot's scan).
+// pool_alloc returns memory any stream may use at once; pool_free returns
+// memory that no queued work uses any more.
+cudaError_t pool_alloc(int device, void **p, size_t bytes);
+cudaError_t pool_free(int device, void *p);
+// a disable-timing event of the device's recycled set, and its return
+cudaError_t event_take(int device, cudaEvent_t *ev);
+void event_give(int device, cudaEvent_t ev);
+
 #define BGO_CUDA(call)                                              \
     do {                                                            \
         cudaError_t _e = (call);                                    \
@@ -221,6 +232,10 @@ struct bgo_plan {
     bgo::MaskArgs mask;
     bgo_tuning tuning;        // launch parameters chosen by the caller (zeros = defaults)
     std::vector<bgo_tuning> fam_tuning;  // per family (split launches); empty = tuning
+    // recorded after the last work that reads the plan's device memory
+    // (creation, scans, graph replays); destroy and index rebuilds wait on it
+    cudaEvent_t done = nullptr;
+    uint64_t index_gen = 0;   // bumped when an index block is replaced
 };
 
 namespace bgo {

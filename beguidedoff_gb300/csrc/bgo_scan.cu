@@ -361,18 +361,22 @@ extern "C" int bgo_plan_create(bgo_engine *engine, const uint64_t *guide_encoded
     pl->tuning = bgo_tuning{};
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = (pl->h_fams && pl->h_guides) ? cudaSuccess : cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) e = cudaSetDevice(engine->device);
+    if (e == cudaSuccess) e = event_take(pl->device, &pl->done);
     if (e == cudaSuccess) {
         std::copy(fams.begin(), fams.end(), pl->h_fams);
         std::copy(recs.begin(), recs.end(), pl->h_guides);
-        e = cudaMalloc(&pl->d_fams, sizeof(FamilyDesc) * (fams.size() + 1));
+        e = pool_alloc(pl->device, (void **)&pl->d_fams, sizeof(FamilyDesc) * (fams.size() + 1));
     }
-    if (e == cudaSuccess) e = cudaMalloc(&pl->d_guides, sizeof(GuideRec) * (recs.size() + 1));
+    if (e == cudaSuccess)
+        e = pool_alloc(pl->device, (void **)&pl->d_guides, sizeof(GuideRec) * (recs.size() + 1));
     if (e == cudaSuccess && !fams.empty())
         e = cudaMemcpyAsync(pl->d_fams, fams.data(), sizeof(FamilyDesc) * fams.size(),
                             cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && !recs.empty())
         e = cudaMemcpyAsync(pl->d_guides, recs.data(), sizeof(GuideRec) * recs.size(),
                             cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaEventRecord(pl->done, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         bgo_plan_destroy(pl);
@@ -386,13 +390,16 @@ extern "C" int bgo_plan_create(bgo_engine *engine, const uint64_t *guide_encoded
 extern "C" int bgo_plan_destroy(bgo_plan *pl) {
     if (!pl) return BGO_OK;
     cudaSetDevice(pl->device);
-    if (pl->d_fams) cudaFree(pl->d_fams);
-    if (pl->d_guides) cudaFree(pl->d_guides);
+    // waits for the plan's last use only, not for the device
+    if (pl->done) cudaEventSynchronize(pl->done);
+    pool_free(pl->device, pl->d_fams);
+    pool_free(pl->device, pl->d_guides);
+    pool_free(pl->device, pl->d_seed);
+    pool_free(pl->device, pl->d_seed_fam);
+    pool_free(pl->device, pl->d_mask);
+    event_give(pl->device, pl->done);
     delete[] pl->h_fams;
     delete[] pl->h_guides;
-    if (pl->d_seed) cudaFree(pl->d_seed);
-    if (pl->d_seed_fam) cudaFree(pl->d_seed_fam);
-    if (pl->d_mask) cudaFree(pl->d_mask);
     delete pl;
     return BGO_OK;
 }
@@ -511,11 +518,12 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
     };
     if (pl->seed_k == K && pl->seed_tols == tols) return applies();
     if (pl->d_seed || pl->d_seed_fam) {
-        BGO_CUDA(cudaStreamSynchronize(s));
-        if (pl->d_seed) cudaFree(pl->d_seed);
-        if (pl->d_seed_fam) cudaFree(pl->d_seed_fam);
+        BGO_CUDA(cudaEventSynchronize(pl->done));  // launches that read the old index
+        BGO_CUDA(pool_free(pl->device, pl->d_seed));
+        BGO_CUDA(pool_free(pl->device, pl->d_seed_fam));
         pl->d_seed = nullptr;
         pl->d_seed_fam = nullptr;
+        pl->index_gen++;
     }
     pl->seed_fam.clear();
     pl->seed_k = K;
@@ -538,7 +546,7 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
     sa.n_guides = pl->n_active;
     sa.n_offsets = (int32_t)offs.size();
     sa.n_lists = (int32_t)ents.size();
-    BGO_CUDA(cudaMalloc(&pl->d_seed, o_i + b_i + 16));
+    BGO_CUDA(pool_alloc(pl->device, (void **)&pl->d_seed, o_i + b_i + 16));
     BGO_CUDA(cudaMemcpyAsync(pl->d_seed, sf.data(), b_f, cudaMemcpyHostToDevice, s));
     if (b_e) {
         BGO_CUDA(cudaMemcpyAsync(pl->d_seed + o_e, ents.data(), b_e, cudaMemcpyHostToDevice, s));
@@ -572,7 +580,8 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
         v.offsets = sa.offsets + off0;
         views[f] = v;
     }
-    BGO_CUDA(cudaMalloc(&pl->d_seed_fam, sizeof(SeedFam) * (rebased.size() + 1)));
+    BGO_CUDA(pool_alloc(pl->device, (void **)&pl->d_seed_fam,
+                        sizeof(SeedFam) * (rebased.size() + 1)));
     BGO_CUDA(cudaMemcpyAsync(pl->d_seed_fam, rebased.data(), sizeof(SeedFam) * rebased.size(),
                              cudaMemcpyHostToDevice, s));
     BGO_CUDA(cudaStreamSynchronize(s));
@@ -596,9 +605,10 @@ static int mask_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
         return pl->mask_ok;
     }
     if (pl->d_mask) {
-        BGO_CUDA(cudaStreamSynchronize(s));
-        cudaFree(pl->d_mask);
+        BGO_CUDA(cudaEventSynchronize(pl->done));  // launches that read the old index
+        BGO_CUDA(pool_free(pl->device, pl->d_mask));
         pl->d_mask = nullptr;
+        pl->index_gen++;
     }
     pl->mask_k = K;
     pl->mask_group = group;
@@ -622,7 +632,7 @@ static int mask_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
     ma.chunk_sites = chunk;
     // the whole index must fit in shared memory beside the warps' chunk slices
     if (mask_smem_bytes(ma) > 220 * 1024) return 0;
-    BGO_CUDA(cudaMalloc(&pl->d_mask, o_d + b_d + 16));
+    BGO_CUDA(pool_alloc(pl->device, (void **)&pl->d_mask, o_d + b_d + 16));
     BGO_CUDA(cudaMemcpyAsync(pl->d_mask, mf.data(), b_f, cudaMemcpyHostToDevice, s));
     if (b_g) BGO_CUDA(cudaMemcpyAsync(pl->d_mask + o_g, groups.data(), b_g, cudaMemcpyHostToDevice, s));
     if (b_t) BGO_CUDA(cudaMemcpyAsync(pl->d_mask + o_t, table.data(), b_t, cudaMemcpyHostToDevice, s));
@@ -638,10 +648,9 @@ static int mask_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
     return 1;
 }
 
-extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
-                               const bgo_genome *const *strands, const int32_t *n_encoded,
-                               int32_t n_strands, int32_t max_mismatches, int32_t mode,
-                               void *stream) {
+static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genome *const *strands,
+                       const int32_t *n_encoded, int32_t n_strands, int32_t max_mismatches,
+                       int32_t mode, void *stream) {
     if (!engine || !plan || !strands || !n_encoded || n_strands < 1 || n_strands > 2 ||
         mode < 0 || mode > 3) {
         set_error("bgo_scan_launch: invalid argument");
@@ -773,6 +782,22 @@ extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
     return BGO_OK;
 }
 
+extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
+                               const bgo_genome *const *strands, const int32_t *n_encoded,
+                               int32_t n_strands, int32_t max_mismatches, int32_t mode,
+                               void *stream) {
+    const int rc = scan_launch(engine, plan, strands, n_encoded, n_strands, max_mismatches, mode,
+                               stream);
+    if (rc != BGO_OK) return rc;
+    // mark the plan's last use (not while a graph is being captured: the
+    // replay records it instead)
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    BGO_CUDA(cudaStreamIsCapturing(s, &cap));
+    if (cap == cudaStreamCaptureStatusNone) BGO_CUDA(cudaEventRecord(plan->done, s));
+    return BGO_OK;
+}
+
 extern "C" int bgo_scan_time(bgo_engine *engine, const bgo_plan *plan,
                              const bgo_genome *const *strands, const int32_t *n_encoded,
                              int32_t n_strands, int32_t max_mismatches, int32_t mode, int32_t reps,
@@ -814,6 +839,7 @@ struct bgo_graph {
     std::vector<int32_t> n_encoded;
     int32_t max_mismatches, mode;
     uint64_t keys_gen;
+    uint64_t plan_gen;  // the plan's index generation the capture used
 };
 
 // Captures one bgo_scan_launch on a private stream (nothing runs).
@@ -843,6 +869,23 @@ static int capture_scan(bgo_graph *g, cudaGraphExec_t *out) {
     return BGO_OK;
 }
 
+// One ordinary launch (builds the index the graph scans with, sets kernel
+// attributes and validates the arguments outside the capture), then the
+// capture.
+static int prepare_and_capture(bgo_graph *g, cudaGraphExec_t *out) {
+    cudaStream_t cs = nullptr;
+    BGO_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    int rc = bgo_scan_launch(g->engine, g->plan, g->strands.data(), g->n_encoded.data(),
+                             (int32_t)g->strands.size(), g->max_mismatches, g->mode, cs);
+    cudaError_t e = rc == BGO_OK ? cudaStreamSynchronize(cs) : cudaSuccess;
+    cudaStreamDestroy(cs);
+    if (rc != BGO_OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "bgo_graph capture");
+    g->keys_gen = g->engine->keys_gen;
+    g->plan_gen = g->plan->index_gen;
+    return capture_scan(g, out);
+}
+
 extern "C" int bgo_graph_create(bgo_engine *engine, const bgo_plan *plan,
                                 const bgo_genome *const *strands, const int32_t *n_encoded,
                                 int32_t n_strands, int32_t max_mismatches, int32_t mode,
@@ -852,18 +895,6 @@ extern "C" int bgo_graph_create(bgo_engine *engine, const bgo_plan *plan,
     if (!engine || !plan || !strands || !n_encoded || n_strands < 1 || n_strands > 2)
         return BGO_ERR_ARG;
     BGO_CUDA(cudaSetDevice(engine->device));
-    // one ordinary launch first: builds the segment index, sets kernel
-    // attributes and validates the arguments outside the capture
-    {
-        cudaStream_t cs = nullptr;
-        BGO_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        int rc = bgo_scan_launch(engine, plan, strands, n_encoded, n_strands, max_mismatches,
-                                 mode, cs);
-        cudaError_t e = rc == BGO_OK ? cudaStreamSynchronize(cs) : cudaSuccess;
-        cudaStreamDestroy(cs);
-        if (rc != BGO_OK) return rc;
-        if (e != cudaSuccess) return cuda_fail(e, "bgo_graph_create");
-    }
     bgo_graph *g = new (std::nothrow) bgo_graph();
     if (!g) return BGO_ERR_OOM;
     g->device = engine->device;
@@ -873,9 +904,8 @@ extern "C" int bgo_graph_create(bgo_engine *engine, const bgo_plan *plan,
     g->n_encoded.assign(n_encoded, n_encoded + n_strands);
     g->max_mismatches = max_mismatches;
     g->mode = mode;
-    g->keys_gen = engine->keys_gen;
     g->exec = nullptr;
-    const int rc = capture_scan(g, &g->exec);
+    const int rc = prepare_and_capture(g, &g->exec);
     if (rc != BGO_OK) {
         delete g;
         return rc;
@@ -887,17 +917,18 @@ extern "C" int bgo_graph_create(bgo_engine *engine, const bgo_plan *plan,
 extern "C" int bgo_graph_launch(bgo_graph *g, void *stream) {
     if (!g) return BGO_ERR_ARG;
     BGO_CUDA(cudaSetDevice(g->device));
-    if (g->keys_gen != g->engine->keys_gen) {
-        // the hit buffer moved (bgo_engine_reserve): the captured kernels
-        // would write to the freed buffer, so capture again
+    if (g->keys_gen != g->engine->keys_gen || g->plan_gen != g->plan->index_gen) {
+        // the hit buffer moved (bgo_engine_reserve) or the plan's index was
+        // rebuilt by a launch with another max_mismatches or tolerance: the
+        // captured kernels would use freed memory, so capture again
         cudaGraphExec_t exec = nullptr;
-        const int rc = capture_scan(g, &exec);
+        const int rc = prepare_and_capture(g, &exec);
         if (rc != BGO_OK) return rc;
         cudaGraphExecDestroy(g->exec);
         g->exec = exec;
-        g->keys_gen = g->engine->keys_gen;
     }
     BGO_CUDA(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+    BGO_CUDA(cudaEventRecord(g->plan->done, (cudaStream_t)stream));
     g->engine->launched = 1;
     g->engine->launches += g->launches_per_replay;
     return BGO_OK;

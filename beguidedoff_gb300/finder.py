@@ -33,7 +33,7 @@ import numpy as np
 
 from . import _native
 from .base_editing import TARGET_2BIT
-from .encoding import encode_dna, encode_guide_64bit, extract_windows
+from .encoding import encode_bytes, encode_dna, encode_guide_64bit, extract_windows
 from .genome_converter import load_genome
 from .io import load_guides_from_tsv
 from .pam import encode_pam_mask
@@ -90,6 +90,7 @@ def prepare_n_masks(genome: dict) -> Tuple[Optional[np.ndarray], Optional[np.nda
 
 
 _ASCII = np.frombuffer(b"ACGT", dtype=np.uint8)
+_GUIDE_SHIFTS = np.arange(0, 40, 2, dtype=np.uint64)
 
 
 def _decode_strings(seq: np.ndarray, pam: np.ndarray, plen: np.ndarray):
@@ -102,6 +103,31 @@ def _decode_strings(seq: np.ndarray, pam: np.ndarray, plen: np.ndarray):
     pa[np.arange(6)[None, :] >= plen[:, None]] = 0   # bytes strings end at the first NUL
     p = np.ascontiguousarray(pa).view("S6").ravel().astype("U6").astype(object)
     return s, p
+
+
+# Output strings and rounded scores are functions of the 20-bit mismatch mask
+# alone, so they are built once per mask and reused across searches.
+_MM_POSITIONS: Dict[int, str] = {}
+_ROUND6: Dict[float, float] = {}
+
+
+def _mismatch_positions(m: int) -> str:
+    """1-based mismatch positions of a mask, "1,5" (encoding.py:94-102)."""
+    out = _MM_POSITIONS.get(m)
+    if out is None:
+        out = ",".join(str(i + 1) for i in range(20) if (m >> i) & 1)
+        _MM_POSITIONS[m] = out
+    return out
+
+
+def _round6(v: float) -> float:
+    """The table's score rounding (round(score, 6), io.py:155-180)."""
+    out = _ROUND6.get(v)
+    if out is None:
+        out = round(v, 6)
+        if len(_ROUND6) < (1 << 21):
+            _ROUND6[v] = out
+    return out
 
 
 def _per_unique(values: np.ndarray, fn) -> np.ndarray:
@@ -257,11 +283,16 @@ class beguidedoff:
 
     def _plan(self, plan_seqs: List[str], plan_pams: List[str], engine=None, stream=None):
         n = len(plan_seqs)
-        gv = np.array([encode_guide_64bit(encode_dna(s)[:20]) for s in plan_seqs],
-                      dtype=np.uint64)
-        pm = np.zeros((n, 6), dtype=np.uint8)
-        for i, pam in enumerate(plan_pams):
-            pm[i] = encode_pam_mask(pam)
+        if n and all(len(s) == 20 for s in plan_seqs):
+            # every row at once: base i of row r at bits 2 * i
+            codes = encode_bytes("".join(plan_seqs).encode("ascii", errors="replace"))
+            gv = np.bitwise_or.reduce(codes.reshape(n, 20).astype(np.uint64)
+                                      << _GUIDE_SHIFTS[None, :], axis=1)
+        else:
+            gv = np.array([encode_guide_64bit(encode_dna(s)[:20]) for s in plan_seqs],
+                          dtype=np.uint64)
+        masks = {p: encode_pam_mask(p) for p in set(plan_pams)}
+        pm = np.stack([masks[p] for p in plan_pams]) if n else np.zeros((0, 6), dtype=np.uint8)
         pl = np.array([len(p) for p in plan_pams], dtype=np.uint8)
         p3 = np.ones(n, dtype=np.uint8)
         return _native.Plan(engine or self._engine, gv, pm, pl, p3, stream)
@@ -559,8 +590,7 @@ class beguidedoff:
         sizes = np.array([b.size for b in blocks], dtype=np.int64)
         idx = np.concatenate(blocks)
         seq_s, pam_s = _decode_strings(seq[idx], pam[idx], plen[idx])
-        mpos = _per_unique(mmask[idx], lambda m: ",".join(str(i + 1) for i in range(20)
-                                                          if (m >> i) & 1))
+        mpos = _per_unique(mmask[idx], _mismatch_positions)
         cols = {
             "guide_rna_sequence": np.array([plan_items[r][0] for r in row[idx].tolist()],
                                            dtype=object),
@@ -574,7 +604,7 @@ class beguidedoff:
             "ot_pam": np.array(pam_s, dtype=object),
             "n_mismatches": mm[idx].astype(np.int64),
             "mismatch_positions": np.array(mpos, dtype=object),
-            "score": _per_unique(score[idx], lambda v: round(float(v), 6)).astype(np.float64),
+            "score": _per_unique(score[idx], _round6).astype(np.float64),
             "n_offtargets_below_threshold": np.repeat(np.array(below, dtype=np.int64), sizes),
         }
         t = Table(cols, COLUMNS)
@@ -691,8 +721,7 @@ class beguidedoff:
         n = idx.size
         seq_s = ["".join(r) for r in _DECODE[seq[idx]]]
         pam_s = ["".join(r[:k]) for r, k in zip(_DECODE[pam[idx]], plen[idx].tolist())]
-        mpos = [",".join(str(i + 1) for i in range(20) if (m >> i) & 1)
-                for m in mmask[idx].tolist()]
+        mpos = [_mismatch_positions(m) for m in mmask[idx].tolist()]
         cols = {
             "guide_rna_sequence": np.array([plan_items[r][0] for r in row[idx].tolist()],
                                            dtype=object),
@@ -706,8 +735,7 @@ class beguidedoff:
             "ot_pam": np.array(pam_s, dtype=object),
             "n_mismatches": mm[idx].astype(np.int64),
             "mismatch_positions": np.array(mpos, dtype=object),
-            "score": np.array([round(float(v), 6) for v in score[idx].tolist()],
-                              dtype=np.float64),
+            "score": np.array([_round6(v) for v in score[idx].tolist()], dtype=np.float64),
             "n_offtargets_below_threshold": np.full(n, n_below, dtype=np.int64),
         }
         return Table(cols, COLUMNS)

@@ -94,9 +94,17 @@ def concat(tables: List[Table]) -> Table:
     return Table({c: np.concatenate([t._cols[c] for t in tables]) for c in cols}, cols)
 
 
+_PANDAS = None
+
+
 def pandas_available():
-    try:
-        import pandas  # noqa: F401
-    except ImportError:
-        return False
-    return True
+    """Whether pandas imports (probed once per process)."""
+    global _PANDAS
+    if _PANDAS is None:
+        try:
+            import pandas  # noqa: F401
+        except ImportError:
+            _PANDAS = False
+        else:
+            _PANDAS = True
+    return _PANDAS

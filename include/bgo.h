@@ -101,6 +101,12 @@ int bgo_engine_destroy(bgo_engine *engine);
  * of PAM position k; pam_lens[i] in 0..6 (0 or >6 = row never matches, as
  * encode_pam_packed leaves its length field 0); pam_3prime[i] 1 = PAM after
  * the guide, 0 = before.  Rows are grouped into PAM families on the device.
+ * A plan's device memory (rows, segment indexes) comes from a stream-ordered
+ * pool the library keeps per device: creating, rebuilding and destroying
+ * plans does not synchronise the device.  bgo_plan_destroy waits for the
+ * plan's last use (its creation, the last bgo_scan_launch or graph replay);
+ * a caller that ran one plan on several streams at once synchronises the
+ * others before destroying it.
  */
 int bgo_plan_create(bgo_engine *engine, const uint64_t *guide_encoded, const uint8_t *pam_masks,
                     const uint8_t *pam_lens, const uint8_t *pam_3prime, int32_t n_guides,
@@ -209,8 +215,10 @@ int bgo_scan_time(bgo_engine *engine, const bgo_plan *plan, const bgo_genome *co
  * synchronises (the segment index, kernel attributes) happens at creation.
  * The graph refers to the engine, plan and strands: keep them alive and
  * unchanged while it exists.  After bgo_engine_reserve moved the hit buffer,
- * the next bgo_graph_launch captures the scan again before it runs.  No
- * reference counterpart: the reference launches one kernel per 200 Mbp chunk.
+ * or after a launch of the plan with another max_mismatches or tolerance
+ * rebuilt its index, the next bgo_graph_launch runs one ordinary scan and
+ * captures the scan again before it replays.  No reference counterpart: the
+ * reference launches one kernel per 200 Mbp chunk.
  */
 typedef struct bgo_graph bgo_graph;
 int bgo_graph_create(bgo_engine *engine, const bgo_plan *plan, const bgo_genome *const *strands,

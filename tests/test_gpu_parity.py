@@ -502,6 +502,45 @@ def test_graph_recaptures_after_hit_buffer_grows():
         f.close()
 
 
+def test_graph_recaptures_after_plan_index_rebuild():
+    """A launch of the same plan with another max_mismatches or tolerance
+    rebuilds (and frees) the index a graph was captured with: the next replay
+    prepares and captures again, and returns the graph's own keys."""
+    genome, rng = _random_genome(58, [500_000, 210_000])
+    seqs, pams = [], []
+    for i in range(40):
+        s = "".join(rng.choice(list("ACGT"), 20))
+        pam = MIXED_PAMS[i % 5]
+        _plant(genome, rng, s, pam, 4, 4)
+        seqs.append(s)
+        pams.append(pam)
+    exp4 = oracle_keys(genome, seqs, pams, 4)
+    exp2 = oracle_keys(genome, seqs, pams, 2)
+    f = beguidedoff(None, max_mismatches=4, genome_data=genome)
+    try:
+        plan = f._plan(seqs, pams)
+        for mode in (2, 3):
+            gr = _native.Graph(f._engine, plan, f._strands, [0, 3], 4, mode)
+            gr.replay()
+            assert np.array_equal(f._engine.collect()[1], exp4), mode
+            # a direct launch at K = 2 rebuilds the plan's index
+            assert np.array_equal(f._engine.scan(plan, f._strands, [0, 3], 2, mode), exp2)
+            gr.replay()
+            assert np.array_equal(f._engine.collect()[1], exp4), mode
+            if mode == 2:
+                # a tolerance change rebuilds it too; the re-capture uses it
+                plan.set_tuning(0, 0, 0, 0, 1, 1)
+                assert np.array_equal(f._engine.scan(plan, f._strands, [0, 3], 4, 2), exp4)
+                plan.set_tuning(0, 0, 0, 0, 0, 0)
+                assert np.array_equal(f._engine.scan(plan, f._strands, [0, 3], 4, 2), exp4)
+                gr.replay()
+                assert np.array_equal(f._engine.collect()[1], exp4)
+            gr.close()
+        plan.close()
+    finally:
+        f.close()
+
+
 def test_strand_upload_in_place_equals_fresh_strands():
     """bgo_genome_upload replaces a resident strand's contents without
     reallocating: scans afterwards see only the new genome."""
