@@ -239,46 +239,43 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
                 const uint64_t pos = (uint64_t)(base + s);
                 // Branch-free in three phases so that the regions' load
                 // chains overlap: (1) every region's bucket descriptor, (2) an
-                // inline compare of every bucket's first guide (an empty
-                // bucket compares its region list's first entry, always
-                // present, and ignores the result), (3) the rare candidates
-                // within K.  Further guides of a bucket stay as a range.
-                // INLINE (1 or 2) guides of each bucket are compared inline;
-                // the rest of a bucket goes through the queue
+                // inline compare of each bucket's first INLINE (1 or 2) entry
+                // slots, (3) the rare candidates within K.  A slot past the
+                // bucket's end is compared too and its result ignored: it is
+                // a later entry or, past the last list, the bucket table that
+                // follows the lists in shared memory, so the load stays in
+                // bounds.  Guides beyond the inline slots are walked by their
+                // lane (WALK) or queued as ranges for the warp.
                 constexpr uint32_t INL = (uint32_t)INLINE;
-                uint32_t rn[S], e0v[S];
-                uint32_t T = 0, R = 0, within = 0, within2 = 0;
+                uint32_t nn[S], e0v[S];
+                uint32_t T = 0, maxn = 0;
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
                     const int st = G::start(j), kl = G::klen(j);
                     const uint32_t km = (1u << kl) - 1u;
                     const uint32_t code = (((h20 >> st) & km) << kl) | ((l20 >> st) & km);
                     const uint32_t d = has ? sOff[seg_off[j] + code] : 0u;
-                    const uint32_t n = d >> 16;
+                    nn[j] = d >> 16;
                     e0v[j] = seg_ent[j] + (d & 0xFFFFu);
-                    T += n;
-                    rn[j] = n > INL ? n - INL : 0u;
-                    R += rn[j] != 0u;
-                    if (n == 0u) e0v[j] = seg_ent[j];
-                    within |= (n != 0u ? 1u : 0u) << j;
-                    if (INL == 2u) within2 |= (n >= 2u ? 1u : 0u) << j;
+                    T += nn[j];
+                    maxn = max(maxn, nn[j]);
                 }
+                uint32_t hit = 0;  // bit j * INL + a: slot a of bucket j is within K
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
-                    const uint2 e = sEnt[e0v[j]];
-                    if (__popc((h20 ^ e.x) | (l20 ^ e.y)) > K) within &= ~(1u << j);
-                    if (INL == 2u) {
-                        // the second entry (the first again when the bucket holds one)
-                        const uint2 e2 = sEnt[e0v[j] + ((within2 >> j) & 1u)];
-                        if (__popc((h20 ^ e2.x) | (l20 ^ e2.y)) > K) within2 &= ~(1u << j);
+#pragma unroll
+                    for (uint32_t a = 0; a < INL; ++a) {
+                        const uint2 e = sEnt[e0v[j] + a];
+                        const bool in = nn[j] > a && __popc((h20 ^ e.x) | (l20 ^ e.y)) <= K;
+                        hit |= (in ? 1u : 0u) << (j * INL + a);
                     }
                 }
-                if (within | within2) {
+                if (hit) {
 #pragma unroll
                     for (int j = 0; j < S; ++j) {
 #pragma unroll
                         for (uint32_t a = 0; a < INL; ++a) {
-                            if (((a == 0u ? within : within2) >> j) & 1u) {
+                            if ((hit >> (j * INL + a)) & 1u) {
                                 const uint32_t ei = e0v[j] + a;
                                 const uint2 e = sEnt[ei];
                                 const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
@@ -289,14 +286,14 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
                     }
                 }
                 cand += T;
-                if (!__any_sync(0xFFFFFFFFu, R != 0u)) continue;
+                if (!__any_sync(0xFFFFFFFFu, maxn > INL)) continue;
                 if constexpr (WALK == 1) {
                     // buckets that rarely hold more than the inline guides:
                     // each lane walks its own few remaining entries
 #pragma unroll
                     for (int j = 0; j < S; ++j) {
-                        for (uint32_t i = 0; i < rn[j]; ++i) {
-                            const uint32_t ei = e0v[j] + INL + i;
+                        for (uint32_t i = INL; i < nn[j]; ++i) {
+                            const uint32_t ei = e0v[j] + i;
                             const uint2 e = sEnt[ei];
                             const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
                             const int cm = __popc(m);
@@ -308,6 +305,9 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
                     continue;
                 }
                 // buckets with more guides: ranges spread over the warp's lanes
+                uint32_t R = 0;
+#pragma unroll
+                for (int j = 0; j < S; ++j) R += nn[j] > INL ? 1u : 0u;
                 uint32_t rin = R;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -319,9 +319,9 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
                 uint32_t qp = rin - R;
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
-                    if (rn[j]) {
+                    if (nn[j] > INL) {
                         wQ[qp] = (e0v[j] + INL) | ((uint32_t)j << 22) | ((uint32_t)lane << 27);
-                        wCnt[qp] = (uint16_t)rn[j];
+                        wCnt[qp] = (uint16_t)(nn[j] - INL);
                         ++qp;
                     }
                 }
