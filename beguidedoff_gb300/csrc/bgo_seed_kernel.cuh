@@ -168,13 +168,8 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
         for (int f = p.fam_begin; f < p.fam_end; ++f) {
             const FamilyDesc F = p.fams[f];
             const uint32_t win_off = F.three_prime ? 0u : (uint32_t)F.plen;
-            const int n_tests = sFam[f - p.fam_begin].n_tests;
-            uint32_t tsh[kMaxPam], tcd[kMaxPam];
-#pragma unroll
-            for (int k = 0; k < kMaxPam; ++k) {
-                tsh[k] = sFam[f - p.fam_begin].pam_shift[k];
-                tcd[k] = sFam[f - p.fam_begin].pam_code[k];
-            }
+            const SeedFam &SF = sFam[f - p.fam_begin];
+            const int n_tests = SF.n_tests;
             uint32_t pass[C::kRows];
             int cnt = 0;
 #pragma unroll
@@ -183,10 +178,11 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
                 const int rem = lim - 32 * wi;
                 uint32_t ps = rem >= 32 ? 0xFFFFFFFFu : (rem <= 0 ? 0u : (1u << rem) - 1u);
                 const uint32_t h0 = wH[wi], h1 = wH[wi + 1], l0 = wL[wi], l1 = wL[wi + 1];
-#pragma unroll
-                for (int k = 0; k < kMaxPam; ++k) {
-                    if (k < n_tests)
-                        ps &= pam_test(sfshr(h0, h1, tsh[k]), sfshr(l0, l1, tsh[k]), tcd[k]);
+                // only the family's own tests run (a loop, not predicated slots)
+#pragma unroll 1
+                for (int k = 0; k < n_tests; ++k) {
+                    const uint32_t sh = SF.pam_shift[k];
+                    ps &= pam_test(sfshr(h0, h1, sh), sfshr(l0, l1, sh), SF.pam_code[k]);
                 }
                 pass[u] = ps;
                 cnt += __popc(ps);
