@@ -90,9 +90,13 @@ struct SeedFam {
     // value, bit1 high-bit compared, bit2 low-bit value, bit3 low-bit compared
     uint8_t n_tests;
     uint8_t pam_shift[kMaxPam];
-    uint8_t pad0;
+    uint8_t pam_generic;  // bit t: test t is a generic allowed-set test
     uint16_t pam_code[kMaxPam];
     uint32_t pad1;
+    // pam_code[t] decoded into whole-word masks (0 or all ones): generic
+    // tests the allowed flag of A, C, G, T; fixed tests high-bit value,
+    // high-bit compared, low-bit value, low-bit compared
+    uint4 pam_mask[kMaxPam];
     SeedSeg seg[kMaxSeg];
 };
 static_assert(sizeof(SeedFam) % 16 == 0, "SeedFam arrays keep 16-byte alignment");

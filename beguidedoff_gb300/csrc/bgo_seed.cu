@@ -89,6 +89,7 @@ int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, in
 void pam_program(const FamilyDesc &F, SeedFam &sf) {
     const uint32_t pam_off = F.three_prime ? 20u : 0u;
     sf.n_tests = 0;
+    sf.pam_generic = 0;
     for (int k = 0; k < F.plen; ++k) {
         const uint32_t a = F.allowed[k] & 15u;
         if (a == 15u) continue;
@@ -109,8 +110,12 @@ void pam_program(const FamilyDesc &F, SeedFam &sf) {
         } else {
             code = (uint16_t)(0x100u | a);
         }
-        sf.pam_shift[sf.n_tests] = (uint8_t)(pam_off + (uint32_t)k);
-        sf.pam_code[sf.n_tests] = code;
+        const int t = sf.n_tests;
+        sf.pam_shift[t] = (uint8_t)(pam_off + (uint32_t)k);
+        sf.pam_code[t] = code;
+        auto all = [](uint32_t bit) { return bit ? 0xFFFFFFFFu : 0u; };
+        sf.pam_mask[t] = make_uint4(all(code & 1u), all(code & 2u), all(code & 4u), all(code & 8u));
+        if (code & 0x100u) sf.pam_generic |= (uint8_t)(1u << t);
         sf.n_tests++;
     }
 }

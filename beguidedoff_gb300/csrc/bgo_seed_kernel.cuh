@@ -182,7 +182,11 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
 #pragma unroll 1
                 for (int k = 0; k < n_tests; ++k) {
                     const uint32_t sh = SF.pam_shift[k];
-                    ps &= pam_test(sfshr(h0, h1, sh), sfshr(l0, l1, sh), SF.pam_code[k]);
+                    const uint4 m = SF.pam_mask[k];
+                    const uint32_t h = sfshr(h0, h1, sh), l = sfshr(l0, l1, sh);
+                    ps &= ((SF.pam_generic >> k) & 1u)
+                              ? (~h & ~l & m.x) | (~h & l & m.y) | (h & ~l & m.z) | (h & l & m.w)
+                              : ~(((h ^ m.x) & m.y) | ((l ^ m.z) & m.w));
                 }
                 pass[u] = ps;
                 cnt += __popc(ps);
