@@ -37,7 +37,7 @@ from .encoding import encode_bytes, encode_dna, encode_guide_64bit, extract_wind
 from .genome_converter import load_genome
 from .io import load_guides_from_tsv
 from .pam import encode_pam_mask
-from .scoring import cctop_from_masks
+from .scoring import scores_of_masks
 from .table import COLUMNS, Table, concat, pandas_available
 from .types import GuideInput
 
@@ -130,10 +130,24 @@ def _round6(v: float) -> float:
     return out
 
 
+def _guide_bases(seqs: List[str]) -> np.ndarray:
+    """[n, 20] 2-bit bases of guide strings (shorter ones zero-padded)."""
+    n = len(seqs)
+    if n and all(len(q) == 20 for q in seqs):
+        return encode_bytes("".join(seqs).encode("ascii", errors="replace")).reshape(n, 20)
+    gb = np.zeros((n, 20), dtype=np.uint8)
+    for i, q in enumerate(seqs):
+        enc = encode_dna(q)[:20]
+        gb[i, :enc.size] = enc
+    return gb
+
+
 def _per_unique(values: np.ndarray, fn) -> np.ndarray:
     """fn applied once per distinct value, spread back (an object array)."""
     if values.size == 0:
         return np.zeros(0, dtype=object)
+    if values.size <= 4096:  # fn is memoised: a direct pass is cheaper than unique
+        return np.array([fn(v) for v in values.tolist()] + [None], dtype=object)[:-1]
     uniq, inv = np.unique(values, return_inverse=True)
     mapped = np.array([fn(v) for v in uniq.tolist()] + [None], dtype=object)[:-1]
     return mapped[inv.ravel()]
@@ -554,14 +568,11 @@ class beguidedoff:
                 seq[sel] = extract_windows(arr, pos[sel], 20)
                 pam[sel] = extract_windows(arr, pos[sel] + 20, 6)
         plen = np.array([len(plan_items[r][1]) for r in row.tolist()], dtype=np.int64)
-        gb = np.zeros((len(plan_items), 20), dtype=np.uint8)
-        for p_i, (gseq, _) in enumerate(plan_items):
-            enc = encode_dna(gseq)[:20]
-            gb[p_i, :enc.size] = enc
+        gb = _guide_bases([g for g, _ in plan_items])
         weights = np.int64(1) << np.arange(20, dtype=np.int64)
         mmask = ((seq != gb[row]).astype(np.int64) * weights[None, :]).sum(1) if n else \
             np.zeros(0, dtype=np.int64)
-        score = cctop_from_masks(mmask)
+        score = scores_of_masks(mmask)
         offsets, lengths = self.chrom_offsets, self.chrom_lengths
         window = 20 + plen
         leftmost = pos.copy()
@@ -572,30 +583,32 @@ class beguidedoff:
         report = np.where(minus, leftmost + window - 1, pos)
         rep_ci = np.searchsorted(offsets, report, side="right") - 1
         rep_local = report - offsets[rep_ci]
-        # one block per input guide row, in input order
-        blocks, editors, below = [], [], []
-        for g in guides:
-            c = gid_code.get(g.guide_id)
-            if c is None or bounds[c] == bounds[c + 1]:
-                continue
-            blocks.append(np.arange(bounds[c], bounds[c + 1]))
-            editors.append(g.base_editor or "")
-            below.append((below_by_id or {}).get(g.guide_id, 0))
-        if not blocks:
+        # one block per input guide row, in input order: the id's kept records
+        codes = np.array([gid_code.get(g.guide_id, -1) for g in guides], dtype=np.int64)
+        cc = np.maximum(codes, 0)
+        sizes = np.where(codes >= 0, bounds[cc + 1] - bounds[cc], 0)
+        rows_in = np.nonzero(sizes)[0]
+        if rows_in.size == 0:
             if pandas_available():
                 import pandas as pd
 
                 return pd.DataFrame()
             return Table()
-        sizes = np.array([b.size for b in blocks], dtype=np.int64)
-        idx = np.concatenate(blocks)
+        sizes = sizes[rows_in]
+        starts = bounds[cc[rows_in]]
+        ends = np.cumsum(sizes)
+        within = np.arange(int(ends[-1]), dtype=np.int64) - np.repeat(ends - sizes, sizes)
+        idx = np.repeat(starts, sizes) + within
+        bid = below_by_id or {}
+        editors = [guides[i].base_editor or "" for i in rows_in.tolist()]
+        below = [bid.get(guides[i].guide_id, 0) for i in rows_in.tolist()]
         seq_s, pam_s = _decode_strings(seq[idx], pam[idx], plen[idx])
         mpos = _per_unique(mmask[idx], _mismatch_positions)
         cols = {
             "guide_rna_sequence": np.array([plan_items[r][0] for r in row[idx].tolist()],
                                            dtype=object),
             "base_editor": np.repeat(np.array(editors, dtype=object), sizes),
-            "ot_rank": np.concatenate([np.arange(1, k + 1, dtype=np.int64) for k in sizes]),
+            "ot_rank": within + 1,
             "ot_chromosome": np.array([self.chrom_names[c] for c in rep_ci[idx].tolist()],
                                       dtype=object),
             "ot_position": (rep_local[idx] + 1).astype(np.int64),
@@ -667,7 +680,7 @@ class beguidedoff:
             enc = encode_dna(plan_items[p_i][0])[:20]
             gb[:enc.size] = enc
             mmask[a:b] = ((seq[a:b] != gb[None, :]).astype(np.int64) * weights[None, :]).sum(1)
-        score = cctop_from_masks(mmask)
+        score = scores_of_masks(mmask)
         include_non_editable = return_all
         below: Dict[str, int] = defaultdict(int)
         if precomputed is not None and precomputed[1] is not None:

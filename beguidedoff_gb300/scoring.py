@@ -45,6 +45,16 @@ def threshold_rank(threshold) -> int:
     return int(np.searchsorted(distinct, float(threshold), side="right")) - 1
 
 
+def scores_of_masks(masks: np.ndarray) -> np.ndarray:
+    """cctop_from_masks through the score-rank table when it is built (the
+    device epilogue builds it): the table's distinct scores are the same
+    float64 values, so the lookup is exact and costs no per-position pass."""
+    if _RANKS is None:
+        return cctop_from_masks(masks)
+    ranks, distinct = _RANKS
+    return distinct[ranks[np.asarray(masks, dtype=np.int64)]]
+
+
 def cctop_from_masks(masks: np.ndarray, compensated: bool = COMPENSATED_SUM) -> np.ndarray:
     """Scores of 20-bit mismatch masks (bit p-1 = position p), equal to
     ``calculate_cctop_score`` of the listed positions."""
