@@ -462,12 +462,17 @@ extern "C" int bgo_epilogue_run(bgo_engine *engine, const bgo_plan *plan,
     if (grow(engine->d_epi, engine->epi_bytes, total) != BGO_OK) return BGO_ERR_CUDA;
     const size_t rank_n = (size_t)1 << 20;
     if (!engine->d_rank) BGO_CUDA(cudaMalloc(&engine->d_rank, sizeof(uint32_t) * rank_n));
-    if (engine->h_rank.size() != rank_n ||
-        memcmp(engine->h_rank.data(), rank_table, sizeof(uint32_t) * rank_n) != 0) {
-        engine->h_rank.assign(rank_table, rank_table + rank_n);
-        BGO_CUDA(cudaMemcpyAsync(engine->d_rank, engine->h_rank.data(), sizeof(uint32_t) * rank_n,
-                                 cudaMemcpyHostToDevice, s));
-        engine->h2d_bytes += (int64_t)(sizeof(uint32_t) * rank_n);
+    // a table at the address of the last one is taken as unchanged (no 4 MB
+    // compare per call); another address is compared and uploaded if it differs
+    if (rank_table != engine->rank_src) {
+        if (engine->h_rank.size() != rank_n ||
+            memcmp(engine->h_rank.data(), rank_table, sizeof(uint32_t) * rank_n) != 0) {
+            engine->h_rank.assign(rank_table, rank_table + rank_n);
+            BGO_CUDA(cudaMemcpyAsync(engine->d_rank, engine->h_rank.data(),
+                                     sizeof(uint32_t) * rank_n, cudaMemcpyHostToDevice, s));
+            engine->h2d_bytes += (int64_t)(sizeof(uint32_t) * rank_n);
+        }
+        engine->rank_src = rank_table;
     }
     unsigned char *d = engine->d_epi;
     size_t o = 0;

@@ -281,6 +281,7 @@ struct bgo_engine {
     int64_t epi_out_n = -1;               // records of the last epilogue (-1: none)
     uint32_t *d_rank = nullptr;
     std::vector<uint32_t> h_rank;   // host copy of what d_rank holds
+    const uint32_t *rank_src = nullptr;  // caller's table address h_rank was taken from
     // bytes copied host -> device and device -> host by engine calls
     int64_t h2d_bytes = 0, d2h_bytes = 0;
     // bumped whenever d_keys / cap change (captured graphs re-capture then)

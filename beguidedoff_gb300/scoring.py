@@ -33,7 +33,11 @@ def score_ranks():
     if _RANKS is None:
         scores = cctop_from_masks(np.arange(1 << 20, dtype=np.int64))
         distinct, inverse = np.unique(scores, return_inverse=True)
-        _RANKS = (np.ascontiguousarray(inverse.astype(np.uint32)), distinct)
+        ranks = np.ascontiguousarray(inverse.astype(np.uint32))
+        # read-only: engines keep a device copy keyed by this array's address
+        ranks.flags.writeable = False
+        distinct.flags.writeable = False
+        _RANKS = (ranks, distinct)
     return _RANKS
 
 

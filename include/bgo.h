@@ -234,8 +234,10 @@ int bgo_graph_destroy(bgo_graph *graph);
  * (the reference's GuideInput after dedup to a plan row).
  *   rank_table[mask]  rank of the exact CCTOP score of each 20-bit mismatch
  *                     mask (bit p-1 = position p) among all distinct scores,
- *                     ascending; 2^20 entries, built on the host (uploaded
- *                     once per engine while it does not change);
+ *                     ascending; 2^20 entries, built on the host.  The
+ *                     engine uploads it once and keeps the address: a table
+ *                     at the last call's address is taken as unchanged, so
+ *                     new contents go in a new buffer;
  *   chrom_rank[c]     rank of chromosome c's name in sorted name order (the
  *                     reference's tie order after the score);
  *   n_top             the reference's top-N rule.
