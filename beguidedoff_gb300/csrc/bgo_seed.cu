@@ -17,18 +17,21 @@
 // no earlier region differs in at most TOL bases, so each (position, guide)
 // hit is emitted once.
 //
-// Layout.  Warps work independently (no CTA barrier after the start): each
+// Layout.  The index (family PAM programs, bucket tables, entry lists) is
+// copied into shared memory once per CTA: CTAs of 256 threads (3 or 4 per SM)
+// or one CTA of 768 threads per SM, so that 24 warps share one copy of a large
+// index.  Warps then work independently (no CTA barrier after the start): each
 // warp takes chunks of 1,024 or 2,048 positions of one strand and copies the
 // next chunk's H/L/N words with cp.async while it works on the current one
-// (double buffering).  Per PAM family it runs the family's compiled PAM test
-// on 32 positions per lane and word (funnel shifts + LOP3), compacts the
-// passing positions with one warp scan, then processes them 32 per round (one
-// per lane): the lane computes its region keys, loads each bucket descriptor
-// and compares the bucket's first guide inline (all lanes in step,
-// predicated); buckets holding more guides leave the rest as a range in the
-// warp's queue, which the warp then works through.  The region layout is a
-// compile-time function of (K, TOL).  Hits are appended with one atomicAdd per
-// warp.
+// (double buffering).  Per PAM family it runs the family's PAM tests on 32
+// positions per lane and word (funnel shifts + LOP3 against host-decoded
+// masks), compacts the passing positions with one warp scan, then processes
+// them 32 per round (one per lane): the lane computes its region keys, loads
+// each bucket descriptor and compares the bucket's first one or two entries
+// inline (all lanes in step, predicated).  Guides beyond those are walked by
+// their lane or spread over the warp as ranges in a queue.  The region layout
+// is a compile-time function of (K, TOL).  Hits are appended with one
+// atomicAdd per warp.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -3,8 +3,7 @@
 // bucket and the warp range queue (bgo_seed.cu) or the per-lane walk
 // (bgo_seed_walk.cu), tolerance 0 with two inline guides (bgo_seed_i2.cu),
 // tolerance 1 with two and the walk (bgo_seed_t1.cu) - so that they compile in
-// parallel.  The algorithm is described at
-// the top of bgo_seed.cu.
+// parallel.  The algorithm is described at the top of bgo_seed.cu.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -16,8 +15,6 @@
 
 namespace bgo {
 
-
-constexpr int kSeedWarps = kSeedThreads / 32;
 constexpr int kQueueCap = 32 * (kSeedMaxK + 1);  // bucket ranges per round
 
 // Per-warp shared-memory slice for chunks of CH positions: two chunk buffers
