@@ -38,12 +38,12 @@ sys.path.insert(0, ROOT)
 METRIC = "guide-site comparisons/s"
 UNIT = "cmp/s"
 # DRAM bytes (read + write) of one segment-index scan of the plain workload
-# at 300 Mbp, from ncu (profiles/scan_seed_kernel_ngg100_300mbp.md, capture 8);
+# at 300 Mbp, from ncu (profiles/scan_seed_kernel_ngg100_300mbp.md, capture 10);
 # traffic grows with the genome, so the line scales it to the run's length
-NCU_TRAFFIC_PLAIN = (300_000_000, 225.144832e6 + 3.241984e6)
+NCU_TRAFFIC_PLAIN = (300_000_000, 225.138944e6 + 3.651072e6)
 # the same capture's integer-pipe figures: the kernel is issue-bound, so these
 # are its roofline in the integer-ALU sense
-NCU_INT_PLAIN = {"issue_active_frac": 0.771, "alu_pipe_active_frac": 0.669,
+NCU_INT_PLAIN = {"issue_active_frac": 0.791, "alu_pipe_active_frac": 0.697,
                  "warps_active_frac": 0.375,
                  "source": "ncu smsp__issue_active, sm__pipe_alu_cycles_active, "
                            "sm__warps_active (pct of peak, active cycles) at 300 Mbp"}
