@@ -42,6 +42,7 @@ CANDIDATES: Tuple[Tuple[str, int, Tuple[int, ...]], ...] = (
     ("segment-index/t1/per-family/1024", 2, (1024, 0, 0, 1, 0, 1, 0)),
     ("segment-index/t1/cta768", 2, (0, 0, 0, 0, 1, 1, 0)),
     ("segment-index/t1/1024/cta768", 2, (1024, 0, 0, 0, 1, 1, 0)),
+    ("segment-index/t1/i1/1024/cta768", 2, (1024, 0, 0, 0, 1, 1, 1)),
     ("segment-index/walk/cta768", 2, (0, 0, 0, 0, 1, 0, 0, 1)),
     ("segment-index/walk/1024/cta768", 2, (1024, 0, 0, 0, 1, 0, 0, 1)),
     ("segment-masks/2048x128", 3, (2048, 128, 0, 0, 0, 0, 0)),
@@ -63,6 +64,8 @@ FAMILY_CANDIDATES = (
     ("index/walk/cta768", 0, 0, 1, 0, 0, 1),
     ("index/t1/cta768", 0, 0, 1, 1, 0, 0),
     ("index/t1/1024/cta768", 0, 1024, 1, 1, 0, 0),
+    ("index/t1/i1/cta768", 0, 0, 1, 1, 1, 0),
+    ("index/t1/i1/1024/cta768", 0, 1024, 1, 1, 1, 0),
 )
 PER_FAMILY_TUNING = (0, 0, 0, 1, 0, 0, 0, 0)
 INDEXED_MAX_K = 7

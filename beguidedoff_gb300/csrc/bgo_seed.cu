@@ -64,6 +64,8 @@ size_t seed_tuning_smem(const SeedArgs &sa, const bgo_tuning &t) {
 
 int launch_seed_t1(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
                    int min_blocks, int ctas_per_sm, cudaStream_t s);
+int launch_seed_t1i1(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
+                     int min_blocks, int ctas_per_sm, cudaStream_t s);
 int launch_seed_t0i2(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
                      int min_blocks, int ctas_per_sm, cudaStream_t s);
 int launch_seed_t0walk(const ScanParams &p, const SeedArgs &sa, int sm_count, int chunk_sites,
@@ -77,7 +79,9 @@ int launch_seed_kernel(const ScanParams &p, const SeedArgs &sa, int sm_count, in
         return BGO_ERR_ARG;
     }
     if (tolerance == 1)
-        return launch_seed_t1(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
+        return inline_entries == 1
+                   ? launch_seed_t1i1(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s)
+                   : launch_seed_t1(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
     if (inline_entries == 2)
         return launch_seed_t0i2(p, sa, sm_count, chunk_sites, min_blocks, ctas_per_sm, s);
     if (range_walk == 1)

@@ -165,9 +165,9 @@ int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
  *   tolerance     mode 2: mismatches allowed in a key region, 0 (K + 1 exact
  *                 regions) or 1 (K / 2 + 1 regions, guides also indexed under
  *                 every single-base substitution of their keys)
- *   inline_entries  mode 2, tolerance 0: guides of each bucket compared inline
- *                 before the range queue, 1 or 2 (0 = 1); tolerance 1 always
- *                 compares 2
+ *   inline_entries  mode 2: guides of each bucket compared inline before the
+ *                 range queue or the walk, 1 or 2; 0 = 1 for tolerance 0 and
+ *                 2 for tolerance 1
  *   range_walk    mode 2, tolerance 0 with one inline guide: the rest of a
  *                 bucket walked by its own lane (1) instead of spread over the
  *                 warp (0); tolerance 1 always walks

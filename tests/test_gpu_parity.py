@@ -203,7 +203,8 @@ def test_indexed_modes_every_k_equal_oracle(k):
                 (0, 0, 0, 0, 0, 1), (1024, 0, 0, 1, 4, 1), (2048, 0, 0, 1, 3, 1),
                 (0, 0, 0, 0, 0, 0, 2), (1024, 0, 0, 1, 4, 0, 2), (0, 0, 0, 0, 0, 0, 0, 1),
                 (1024, 0, 0, 1, 4, 0, 0, 1), (0, 0, 0, 0, 1, 1), (1024, 0, 0, 1, 1, 1),
-                (0, 0, 0, 0, 1, 0, 0, 1), (2048, 0, 0, 0, 1, 0, 2)]
+                (0, 0, 0, 0, 1, 0, 0, 1), (2048, 0, 0, 0, 1, 0, 2), (0, 0, 0, 0, 1, 1, 1),
+                (1024, 0, 0, 1, 3, 1, 1)]
         for mode, tune in [(2, t) for t in seed] + [(3, t) for t in tunings]:
             plan.set_tuning(*tune)
             got = f._engine.scan(plan, f._strands, [0, 3], k, mode)
@@ -214,7 +215,8 @@ def test_indexed_modes_every_k_equal_oracle(k):
         assert fam.min() >= 0 and fam.max() == len(MIXED_PAMS) - 1
         forms = [dict(form=1), dict(tolerance=1, chunk_sites=1024), dict(min_blocks=4),
                  dict(tolerance=1, min_blocks=4), dict(chunk_sites=1024, inline_entries=2),
-                 dict(tolerance=1, min_blocks=1), dict(min_blocks=1, range_walk=1)]
+                 dict(tolerance=1, min_blocks=1), dict(min_blocks=1, range_walk=1),
+                 dict(tolerance=1, inline_entries=1, chunk_sites=1024, min_blocks=1)]
         for fi in range(fam.max() + 1):
             plan.set_family_tuning(fi, **forms[fi % len(forms)])
         got = f._engine.scan(plan, f._strands, [0, 3], k, 2)
