@@ -373,17 +373,7 @@ class beguidedoff:
             t1 = time.perf_counter()
             ne = [0, 3][:len(self._strands)]
             eng.launch(plan, self._strands, ne, max_mismatches, mode, stream)
-            n = eng.hit_count(stream)
-            if n > eng.info()["hit_capacity"]:
-                eng.reserve(n)
-                eng.launch(plan, self._strands, ne, max_mismatches, mode, stream)
-            t2 = time.perf_counter()
-            # this batch's own record (batches of several serving slots run
-            # concurrently; last_batch only ever receives a finished record)
-            stats = {"hits": n, "plan_rows": len(plan_items), "mode": mode,
-                     "plan_s": t1 - t0, "scan_s": t2 - t1}
-            if info is not None:
-                info.update(stats)
+            # the epilogue's input rows are built on the host while the scan runs
             parts, owners, spans, errs = [], [], [], []
             n_rows = 0
             for r in reqs:
@@ -405,6 +395,17 @@ class beguidedoff:
                 n_rows += len(pairs)
                 parts.append(rows)
                 owners.append([g.guide_id for _, g, _ in pairs])
+            n = eng.hit_count(stream)
+            if n > eng.info()["hit_capacity"]:
+                eng.reserve(n)
+                eng.launch(plan, self._strands, ne, max_mismatches, mode, stream)
+            t2 = time.perf_counter()
+            # this batch's own record (batches of several serving slots run
+            # concurrently; last_batch only ever receives a finished record)
+            stats = {"hits": n, "plan_rows": len(plan_items), "mode": mode,
+                     "plan_s": t1 - t0, "scan_s": t2 - t1}
+            if info is not None:
+                info.update(stats)
             full = None
             if parts:
                 rank_table, _ = score_ranks()
