@@ -97,3 +97,53 @@ def test_requests_equal_alone_and_in_the_mix():
     finally:
         for f in alone.values():
             f.close()
+
+
+def test_plans_created_and_destroyed_on_two_streams_at_once():
+    """Two threads, each with its own engine and stream, create, scan and
+    destroy plans in a loop while the other's scans run (plan memory comes
+    from the library's pool; destroy waits for the plan's own last use only):
+    every scan returns the keys of the same plan scanned alone."""
+    g = _genome()
+    f = beguidedoff(None, max_mismatches=4, genome_data=g)
+    try:
+        rng = np.random.default_rng(5)
+        sets = []
+        for t in range(2):
+            seqs = ["".join(rng.choice(list("ACGT"), 20)) for _ in range(24 + 8 * t)]
+            pams = [PAMS[i % len(PAMS)] for i in range(len(seqs))]
+            sets.append((seqs, pams))
+        expected = []
+        for seqs, pams in sets:
+            plan = f._plan(seqs, pams)
+            expected.append(f._engine.scan(plan, f._strands, [0, 3], 4, 2))
+            plan.close()
+        errors = []
+
+        def worker(t):
+            eng = _native.Engine(0)
+            st = _native.Stream(0)
+            try:
+                seqs, pams = sets[t]
+                for it in range(12):
+                    plan = f._plan(seqs, pams, eng, st.handle)
+                    plan.set_tuning(1024 if it % 2 else 0, 0, 0, 0, 1 if it % 3 else 3,
+                                    it % 2)
+                    keys = eng.scan(plan, f._strands, [0, 3], 4, 2, st.handle)
+                    plan.close()
+                    if not np.array_equal(keys, expected[t]):
+                        errors.append((t, it))
+            except Exception as exc:  # reported by the main thread
+                errors.append((t, repr(exc)))
+            finally:
+                st.close()
+                eng.close()
+
+        threads = [threading.Thread(target=worker, args=(t,)) for t in range(2)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        assert not errors, errors
+    finally:
+        f.close()
