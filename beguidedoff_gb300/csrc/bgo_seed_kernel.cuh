@@ -18,7 +18,8 @@ namespace bgo {
 constexpr int kQueueCap = 32 * (kSeedMaxK + 1);  // bucket ranges per round
 
 // Per-warp shared-memory slice for chunks of CH positions: two chunk buffers
-// (H, L, N planes), the compacted list, and, unless the lanes walk their own
+// (H, L, N planes), the compacted list of passing positions, and, unless the
+// lanes walk their own
 // leftover guides (WALK), the round's position records and the bucket-range
 // queue (word + count).
 template <int CH, int WALK>
@@ -28,7 +29,11 @@ struct SeedChunk {
     static constexpr int kVecs = kWords / 4;     // 16-byte copies per plane
     static constexpr size_t kBuf = 3 * kWords * sizeof(uint32_t);
     static constexpr size_t kListOff = 2 * kBuf;
-    static constexpr size_t kRecOff = (kListOff + CH * sizeof(uint16_t) + 15) / 16 * 16;
+    // the list holds up to 1,024 positions; a 2,048-position chunk with more
+    // passing positions is worked through in two passes
+    static constexpr int kListCap = CH < 1024 ? CH : 1024;
+    static constexpr int kPasses = CH / kListCap;
+    static constexpr size_t kRecOff = (kListOff + kListCap * sizeof(uint16_t) + 15) / 16 * 16;
     static constexpr size_t kQueueOff = kRecOff + 32 * sizeof(uint4);
     static constexpr size_t kCountOff = kQueueOff + kQueueCap * sizeof(uint32_t);
     static constexpr size_t kSlice =
@@ -195,17 +200,7 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
                 if (lane >= o) incl += v;
             }
             const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            int off = incl - cnt;
-#pragma unroll
-            for (int u = 0; u < C::kRows; ++u) {
-                uint32_t m = pass[u];
-                while (m) {
-                    const int j = __ffs(m) - 1;
-                    m &= m - 1u;
-                    wList[off++] = (uint16_t)(32 * (u * 32 + lane) + j);
-                }
-            }
-            __syncwarp();
+            const int off0 = incl - cnt;
             // the family's bucket tables and entry bases, held in registers
             uint32_t seg_off[S], seg_ent[S];
             {
@@ -217,130 +212,164 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
                 }
             }
             const uint32_t gbeg = (uint32_t)F.gbeg;
-            for (int k0 = 0; k0 < total; k0 += 32) {
-                const int k = k0 + lane;
-                const bool has = k < total;
-                uint32_t s = 0, h20 = 0, l20 = 0, n20g = 0;
-                if (has) {
-                    s = wList[k];
-                    const uint32_t wo = s + win_off;
-                    const uint32_t wi = wo >> 5, b = wo & 31u;
-                    h20 = sfshr(wH[wi], wH[wi + 1], b) & 0xFFFFFu;
-                    l20 = sfshr(wL[wi], wL[wi + 1], b) & 0xFFFFFu;
-                    if (has_n) {
-                        const uint32_t n26 =
-                            sfshr(wN[s >> 5], wN[(s >> 5) + 1], s & 31u) & 0x3FFFFFFu;
-                        if (n26) n20g = sfshr(wN[wi], wN[wi + 1], b) & 0xFFFFFu;
+#pragma unroll 1
+            for (int pass_i = 0; pass_i < C::kPasses; ++pass_i) {
+                const int lo = pass_i * C::kListCap;
+                if (lo >= total) break;
+                const int n_list = min(total - lo, C::kListCap);
+                // list positions [lo, lo + n_list) of the chunk's passing positions
+                if (C::kPasses == 1) {
+                    int off = off0;
+#pragma unroll
+                    for (int u = 0; u < C::kRows; ++u) {
+                        uint32_t m = pass[u];
+                        while (m) {
+                            const int j = __ffs(m) - 1;
+                            m &= m - 1u;
+                            wList[off++] = (uint16_t)(32 * (u * 32 + lane) + j);
+                        }
+                    }
+                } else if (off0 + cnt > lo && off0 < lo + n_list) {
+                    int off = off0 - lo;
+#pragma unroll
+                    for (int u = 0; u < C::kRows; ++u) {
+                        uint32_t m = pass[u];
+                        while (m) {
+                            const int j = __ffs(m) - 1;
+                            m &= m - 1u;
+                            if ((unsigned)off < (unsigned)n_list)
+                                wList[off] = (uint16_t)(32 * (u * 32 + lane) + j);
+                            ++off;
+                        }
                     }
                 }
-                const uint64_t pos = (uint64_t)(base + s);
-                // Branch-free in three phases so that the regions' load
-                // chains overlap: (1) every region's bucket descriptor, (2) an
-                // inline compare of each bucket's first INLINE (1 or 2) entry
-                // slots, (3) the rare candidates within K.  A slot past the
-                // bucket's end is compared too and its result ignored: it is
-                // a later entry or, past the last list, the bucket table that
-                // follows the lists in shared memory, so the load stays in
-                // bounds.  Guides beyond the inline slots are walked by their
-                // lane (WALK) or queued as ranges for the warp.
-                constexpr uint32_t INL = (uint32_t)INLINE;
-                uint32_t nn[S], e0v[S];
-                uint32_t T = 0, maxn = 0;
-#pragma unroll
-                for (int j = 0; j < S; ++j) {
-                    const int st = G::start(j), kl = G::klen(j);
-                    const uint32_t km = (1u << kl) - 1u;
-                    const uint32_t code = (((h20 >> st) & km) << kl) | ((l20 >> st) & km);
-                    const uint32_t d = has ? sOff[seg_off[j] + code] : 0u;
-                    nn[j] = d >> 16;
-                    e0v[j] = seg_ent[j] + (d & 0xFFFFu);
-                    T += nn[j];
-                    maxn = max(maxn, nn[j]);
-                }
-                uint32_t hit = 0;  // bit j * INL + a: slot a of bucket j is within K
-#pragma unroll
-                for (int j = 0; j < S; ++j) {
-#pragma unroll
-                    for (uint32_t a = 0; a < INL; ++a) {
-                        const uint2 e = sEnt[e0v[j] + a];
-                        const bool in = nn[j] > a && __popc((h20 ^ e.x) | (l20 ^ e.y)) <= K;
-                        hit |= (in ? 1u : 0u) << (j * INL + a);
+                __syncwarp();
+                for (int k0 = 0; k0 < n_list; k0 += 32) {
+                    const int k = k0 + lane;
+                    const bool has = k < n_list;
+                    uint32_t s = 0, h20 = 0, l20 = 0, n20g = 0;
+                    if (has) {
+                        s = wList[k];
+                        const uint32_t wo = s + win_off;
+                        const uint32_t wi = wo >> 5, b = wo & 31u;
+                        h20 = sfshr(wH[wi], wH[wi + 1], b) & 0xFFFFFu;
+                        l20 = sfshr(wL[wi], wL[wi + 1], b) & 0xFFFFFu;
+                        if (has_n) {
+                            const uint32_t n26 =
+                                sfshr(wN[s >> 5], wN[(s >> 5) + 1], s & 31u) & 0x3FFFFFFu;
+                            if (n26) n20g = sfshr(wN[wi], wN[wi + 1], b) & 0xFFFFFu;
+                        }
                     }
-                }
-                if (hit) {
+                    const uint64_t pos = (uint64_t)(base + s);
+                    // Branch-free in three phases so that the regions' load
+                    // chains overlap: (1) every region's bucket descriptor, (2) an
+                    // inline compare of each bucket's first INLINE (1 or 2) entry
+                    // slots, (3) the rare candidates within K.  A slot past the
+                    // bucket's end is compared too and its result ignored: it is
+                    // a later entry or, past the last list, the bucket table that
+                    // follows the lists in shared memory, so the load stays in
+                    // bounds.  Guides beyond the inline slots are walked by their
+                    // lane (WALK) or queued as ranges for the warp.
+                    constexpr uint32_t INL = (uint32_t)INLINE;
+                    uint32_t nn[S], e0v[S];
+                    uint32_t T = 0, maxn = 0;
+#pragma unroll
+                    for (int j = 0; j < S; ++j) {
+                        const int st = G::start(j), kl = G::klen(j);
+                        const uint32_t km = (1u << kl) - 1u;
+                        const uint32_t code = (((h20 >> st) & km) << kl) | ((l20 >> st) & km);
+                        const uint32_t d = has ? sOff[seg_off[j] + code] : 0u;
+                        nn[j] = d >> 16;
+                        e0v[j] = seg_ent[j] + (d & 0xFFFFu);
+                        T += nn[j];
+                        maxn = max(maxn, nn[j]);
+                    }
+                    uint32_t hit = 0;  // bit j * INL + a: slot a of bucket j is within K
 #pragma unroll
                     for (int j = 0; j < S; ++j) {
 #pragma unroll
                         for (uint32_t a = 0; a < INL; ++a) {
-                            if ((hit >> (j * INL + a)) & 1u) {
-                                const uint32_t ei = e0v[j] + a;
-                                const uint2 e = sEnt[ei];
-                                const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
-                                finish_candidate<K, TOL>(p, m, __popc(m), e, sIdx[ei], j, n20g,
-                                                         ne, slot, pos, gbeg);
+                            const uint2 e = sEnt[e0v[j] + a];
+                            const bool in = nn[j] > a && __popc((h20 ^ e.x) | (l20 ^ e.y)) <= K;
+                            hit |= (in ? 1u : 0u) << (j * INL + a);
+                        }
+                    }
+                    if (hit) {
+#pragma unroll
+                        for (int j = 0; j < S; ++j) {
+#pragma unroll
+                            for (uint32_t a = 0; a < INL; ++a) {
+                                if ((hit >> (j * INL + a)) & 1u) {
+                                    const uint32_t ei = e0v[j] + a;
+                                    const uint2 e = sEnt[ei];
+                                    const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
+                                    finish_candidate<K, TOL>(p, m, __popc(m), e, sIdx[ei], j, n20g,
+                                                             ne, slot, pos, gbeg);
+                                }
                             }
                         }
                     }
-                }
-                cand += T;
-                if (!__any_sync(0xFFFFFFFFu, maxn > INL)) continue;
-                if constexpr (WALK == 1) {
-                    // buckets that rarely hold more than the inline guides:
-                    // each lane walks its own few remaining entries
+                    cand += T;
+                    if (!__any_sync(0xFFFFFFFFu, maxn > INL)) continue;
+                    if constexpr (WALK == 1) {
+                        // buckets that rarely hold more than the inline guides:
+                        // each lane walks its own few remaining entries
+#pragma unroll
+                        for (int j = 0; j < S; ++j) {
+                            for (uint32_t i = INL; i < nn[j]; ++i) {
+                                const uint32_t ei = e0v[j] + i;
+                                const uint2 e = sEnt[ei];
+                                const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
+                                const int cm = __popc(m);
+                                if (cm <= K)
+                                    finish_candidate<K, TOL>(p, m, cm, e, sIdx[ei], j, n20g,
+                                                             ne, slot, pos, gbeg);
+                            }
+                        }
+                        continue;
+                    }
+                    // buckets with more guides: ranges spread over the warp's lanes
+                    uint32_t R = 0;
+#pragma unroll
+                    for (int j = 0; j < S; ++j) R += nn[j] > INL ? 1u : 0u;
+                    uint32_t rin = R;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, rin, o);
+                        if (lane >= o) rin += v;
+                    }
+                    const uint32_t RT = __shfl_sync(0xFFFFFFFFu, rin, 31);
+                    wRec[lane] = make_uint4(h20, l20, n20g, s);
+                    uint32_t qp = rin - R;
 #pragma unroll
                     for (int j = 0; j < S; ++j) {
-                        for (uint32_t i = INL; i < nn[j]; ++i) {
-                            const uint32_t ei = e0v[j] + i;
-                            const uint2 e = sEnt[ei];
-                            const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
-                            const int cm = __popc(m);
-                            if (cm <= K)
-                                finish_candidate<K, TOL>(p, m, cm, e, sIdx[ei], j, n20g, ne, slot,
-                                                         pos, gbeg);
+                        if (nn[j] > INL) {
+                            wQ[qp] = (e0v[j] + INL) | ((uint32_t)j << 22) | ((uint32_t)lane << 27);
+                            wCnt[qp] = (uint16_t)(nn[j] - INL);
+                            ++qp;
                         }
                     }
-                    continue;
-                }
-                // buckets with more guides: ranges spread over the warp's lanes
-                uint32_t R = 0;
-#pragma unroll
-                for (int j = 0; j < S; ++j) R += nn[j] > INL ? 1u : 0u;
-                uint32_t rin = R;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, rin, o);
-                    if (lane >= o) rin += v;
-                }
-                const uint32_t RT = __shfl_sync(0xFFFFFFFFu, rin, 31);
-                wRec[lane] = make_uint4(h20, l20, n20g, s);
-                uint32_t qp = rin - R;
-#pragma unroll
-                for (int j = 0; j < S; ++j) {
-                    if (nn[j] > INL) {
-                        wQ[qp] = (e0v[j] + INL) | ((uint32_t)j << 22) | ((uint32_t)lane << 27);
-                        wCnt[qp] = (uint16_t)(nn[j] - INL);
-                        ++qp;
+                    __syncwarp();
+                    for (uint32_t q = lane; q < RT; q += 32) {
+                        const uint32_t v = wQ[q];
+                        const uint32_t n = wCnt[q];
+                        const uint4 r = wRec[v >> 27];
+                        const uint32_t e0 = v & 0x3FFFFFu;
+                        const int j = (int)((v >> 22) & 31u);
+                        for (uint32_t i = 0; i < n; ++i) {
+                            const uint2 e = sEnt[e0 + i];
+                            const uint32_t m = (r.x ^ e.x) | (r.y ^ e.y);
+                            const int cm = __popc(m);
+                            if (cm <= K)
+                                finish_candidate<K, TOL>(p, m, cm, e, sIdx[e0 + i], j, r.z,
+                                                         ne, slot, (uint64_t)(base + r.w),
+                                                         gbeg);
+                        }
                     }
+                    __syncwarp();
                 }
-                __syncwarp();
-                for (uint32_t q = lane; q < RT; q += 32) {
-                    const uint32_t v = wQ[q];
-                    const uint32_t n = wCnt[q];
-                    const uint4 r = wRec[v >> 27];
-                    const uint32_t e0 = v & 0x3FFFFFu;
-                    const int j = (int)((v >> 22) & 31u);
-                    for (uint32_t i = 0; i < n; ++i) {
-                        const uint2 e = sEnt[e0 + i];
-                        const uint32_t m = (r.x ^ e.x) | (r.y ^ e.y);
-                        const int cm = __popc(m);
-                        if (cm <= K)
-                            finish_candidate<K, TOL>(p, m, cm, e, sIdx[e0 + i], j, r.z, ne, slot,
-                                                (uint64_t)(base + r.w), gbeg);
-                    }
-                }
-                __syncwarp();
+                __syncwarp();  // the next pass overwrites the list
             }
-            __syncwarp();
         }
     }
     cp_async_wait<0>();
