@@ -27,7 +27,7 @@ import threading
 import time
 from collections import defaultdict
 from pathlib import Path
-from typing import Dict, List, Optional, Tuple
+from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -191,7 +191,7 @@ class beguidedoff:
                  device: Optional[str] = None, n_top_offtargets: int = 3,
                  results_per_guide: int = 10240, max_results_per_guide: Optional[int] = None,
                  genome_data: Optional[dict] = None, scan_mode="auto",
-                 epilogue: str = "device"):
+                 epilogue: str = "device", scan_tuning: Optional[Sequence[int]] = None):
         if epilogue not in ("device", "host"):
             raise ValueError("epilogue must be 'device' or 'host'")
         self.epilogue = epilogue
@@ -206,6 +206,9 @@ class beguidedoff:
         if scan_mode != "auto" and scan_mode not in (0, 1, 2, 3):
             raise ValueError("scan_mode must be 'auto' or 0..3")
         self.scan_mode = scan_mode
+        # with a fixed scan_mode: the launch parameters every plan gets
+        # (Plan.set_tuning's positional fields); None keeps the defaults
+        self.scan_tuning = tuple(scan_tuning) if scan_tuning is not None else None
         self._tuner = None
         self._tuner_lock = threading.Lock()
         self.last_choice = None
@@ -315,6 +318,8 @@ class beguidedoff:
         """The scan mode to run: the constructor's, or the autotuner's choice
         (which also sets the plan's launch tuning)."""
         if self.scan_mode != "auto":
+            if self.scan_tuning is not None:
+                plan.set_tuning(*self.scan_tuning)
             return int(self.scan_mode)
         k = self.max_mismatches if max_mismatches is None else max_mismatches
         with self._tuner_lock:

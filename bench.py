@@ -38,12 +38,12 @@ sys.path.insert(0, ROOT)
 METRIC = "guide-site comparisons/s"
 UNIT = "cmp/s"
 # DRAM bytes (read + write) of one segment-index scan of the plain workload
-# at 300 Mbp, from ncu (profiles/scan_seed_kernel_ngg100_300mbp.md, capture 10);
+# at 300 Mbp, from ncu (profiles/scan_seed_kernel_ngg100_300mbp.md, capture 12);
 # traffic grows with the genome, so the line scales it to the run's length
-NCU_TRAFFIC_PLAIN = (300_000_000, 225.138944e6 + 3.651072e6)
+NCU_TRAFFIC_PLAIN = (300_000_000, 225.145344e6 + 3.75808e6)
 # the same capture's integer-pipe figures: the kernel is issue-bound, so these
 # are its roofline in the integer-ALU sense
-NCU_INT_PLAIN = {"issue_active_frac": 0.791, "alu_pipe_active_frac": 0.697,
+NCU_INT_PLAIN = {"issue_active_frac": 0.773, "alu_pipe_active_frac": 0.679,
                  "warps_active_frac": 0.375,
                  "source": "ncu smsp__issue_active, sm__pipe_alu_cycles_active, "
                            "sm__warps_active (pct of peak, active cycles) at 300 Mbp"}
@@ -366,8 +366,12 @@ def bench_ours(args, ws, rank, local):
     guides, pams = select_families(args, guides, pams)
     args.guides = len(guides)
     t0 = time.perf_counter()
+    # a fixed mode runs every search() with the command line's launch tuning
+    tuning = (args.chunk_sites, args.group_guides, args.ctas_per_sm, args.split_families,
+              args.min_blocks, args.tolerance, args.inline_entries, args.range_walk)
     f = beguidedoff(None, max_mismatches=args.max_mm, genome_data=genome,
-                    device=f"cuda:{local}", scan_mode=args.mode)
+                    device=f"cuda:{local}", scan_mode=args.mode,
+                    scan_tuning=None if args.mode == "auto" else tuning)
     t_init = time.perf_counter() - t0
     nm_pin = []
     for m in (f._n_mask_fwd, f._n_mask_rc):
@@ -383,9 +387,7 @@ def bench_ours(args, ws, rank, local):
         autotune = dict(f.last_choice.as_dict(), seconds=time.perf_counter() - t0)
         args.mode = f.last_choice.mode
     else:
-        plan.set_tuning(args.chunk_sites, args.group_guides, args.ctas_per_sm,
-                        args.split_families, args.min_blocks, args.tolerance, args.inline_entries,
-                        args.range_walk)
+        plan.set_tuning(*tuning)
     if dense:
         editors = [DENSE_EDITORS[i % 3] for i in range(len(guides))]
     else:
