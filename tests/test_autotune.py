@@ -65,3 +65,55 @@ def test_coarse_signature_classes():
     assert A.coarse_signature(17, 4) == (4, 1)
     assert A.coarse_signature(300, 5) == (5, 3)
     assert A.coarse_signature(5000, 3) == (3, 4)
+
+
+def test_candidate_tunings_are_valid_and_distinct():
+    """Every candidate passes the C ABI's tuning rules (bgo_plan_set_tuning)
+    and names a distinct form, for single launches and per family."""
+    seen = set()
+    for name, mode, tune in A.CANDIDATES:
+        t = dict(zip(A.TUNING_FIELDS, tuple(tune) + (0,) * (len(A.TUNING_FIELDS) - len(tune))))
+        assert mode in (1, 2, 3), name
+        assert t["chunk_sites"] in (0, 1024, 2048), name
+        assert t["group_guides"] in (0, 32, 64, 128), name
+        assert t["split_families"] in (0, 1) and t["tolerance"] in (0, 1), name
+        assert t["min_blocks"] in (0, 1, 3, 4), name
+        assert t["inline_entries"] in (0, 1, 2) and t["range_walk"] in (0, 1), name
+        key = (mode, tuple(t.values()))
+        assert key not in seen, name
+        seen.add(key)
+    fam_seen = set()
+    for name, form, chunk, minb, tol, inl, walk in A.FAMILY_CANDIDATES:
+        assert form in (0, 1) and chunk in (0, 1024, 2048) and minb in (0, 1, 3, 4), name
+        assert tol in (0, 1) and inl in (0, 1, 2) and walk in (0, 1), name
+        assert (form, chunk, minb, tol, inl, walk) not in fam_seen, name
+        fam_seen.add((form, chunk, minb, tol, inl, walk))
+
+
+def test_per_family_choice_applies_each_familys_form():
+    """A per-family choice sets split launches on the plan and each PAM
+    family's own form; a family the choice does not know keeps the plan's
+    defaults."""
+    import numpy as np
+
+    class Plan(FakePlan):
+        def __init__(self):
+            super().__init__()
+            self.fam_calls = {}
+
+        def families(self):
+            return np.array([0, 1, 0, 2, -1], dtype=np.int32)
+
+        def set_family_tuning(self, f, **kw):
+            self.fam_calls[f] = kw
+
+    fam = {"NGG": ("index/t1/cta768", 0, 0, 1, 1, 0, 0, 0.2),
+           "NRN": ("every-guide", 1, 0, 0, 0, 0, 0, 0.5)}
+    ch = A.Choice("per-family", 2, A.PER_FAMILY_TUNING, {}, 0, fam)
+    plan = Plan()
+    ch.apply(plan, ["NGG", "NRN", "ngg", "NNGRRT", "NG"])
+    assert plan.tunings[-1] == A.PER_FAMILY_TUNING
+    assert plan.fam_calls[0] == dict(chunk_sites=0, min_blocks=1, tolerance=1, form=0,
+                                     inline_entries=0, range_walk=0)
+    assert plan.fam_calls[1]["form"] == 1
+    assert 2 not in plan.fam_calls
