@@ -83,8 +83,9 @@ class Choice:
     family: Dict[str, tuple] = field(default_factory=dict)
 
     def as_dict(self):
+        tuning = tuple(self.tuning) + (0,) * (len(TUNING_FIELDS) - len(self.tuning))
         return {"name": self.name, "mode": self.mode,
-                "tuning": dict(zip(TUNING_FIELDS, self.tuning)),
+                "tuning": dict(zip(TUNING_FIELDS, tuning)),
                 "times_ms": {k: round(v, 4) for k, v in self.times_ms.items()},
                 "family": {p: {"form": c[0], "ms": round(c[7], 4)} for p, c in
                            self.family.items()},
