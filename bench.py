@@ -559,7 +559,15 @@ def bench_ours(args, ws, rank, local):
                                       "300 Mbp, scaled by genome length" if traffic else None,
                     "bytes_per_step": plane_bytes,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-                    "int_popc": popc, "int_pipes_ncu": int_pipes}
+                    "int_popc": popc, "int_pipes_ncu": int_pipes,
+                    # the brute-force formulation's integer roofline: 12 INT32 ops
+                    # per guide-site comparison against the measured LOP3 rate; the
+                    # index skips most comparisons, so the ratio exceeds 1
+                    "bruteforce_equivalent": {
+                        "ops_per_comparison": 12,
+                        "achieved_tops": 12 * value / ws / 1e12,
+                        "peak_tops": lop3_peak / 1e3,
+                        "ratio": 12 * value / ws / 1e9 / lop3_peak}}
         else:
             roof = {"bound": "int", "unit": "Gop/s", "achieved": achieved, "peak": popc_peak,
                     "frac": achieved / popc_peak, "traffic": None,
