@@ -159,7 +159,13 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
         const bool second = c >= chunks0;
         const int64_t lc = second ? c - chunks0 : c;
         const int64_t total_bp = second ? p.strand[1].total_bp : p.strand[0].total_bp;
-        const int has_n = second ? p.strand[1].has_n : p.strand[0].has_n;
+        // the N correction applies only in chunks whose words hold an N
+        int has_n = second ? p.strand[1].has_n : p.strand[0].has_n;
+        if (has_n) {
+            uint32_t nw = 0;
+            for (int i = lane; i < C::kWords; i += 32) nw |= wN[i];
+            has_n = __any_sync(0xFFFFFFFFu, nw != 0u);
+        }
         const uint32_t ne = (uint32_t)(second ? p.strand[1].n_encoded : p.strand[0].n_encoded);
         const uint64_t slot = (uint64_t)(second ? p.strand[1].slot : p.strand[0].slot);
         const int64_t base = lc * CH;
