@@ -38,12 +38,12 @@ sys.path.insert(0, ROOT)
 METRIC = "guide-site comparisons/s"
 UNIT = "cmp/s"
 # DRAM bytes (read + write) of one segment-index scan of the plain workload
-# at 300 Mbp, from ncu (profiles/scan_seed_kernel_ngg100_300mbp.md, capture 12);
+# at 300 Mbp, from ncu (profiles/scan_seed_kernel_ngg100_300mbp.md, capture 13);
 # traffic grows with the genome, so the line scales it to the run's length
-NCU_TRAFFIC_PLAIN = (300_000_000, 225.145344e6 + 3.75808e6)
+NCU_TRAFFIC_PLAIN = (300_000_000, 225.173248e6 + 3.749376e6)
 # the same capture's integer-pipe figures: the kernel is issue-bound, so these
 # are its roofline in the integer-ALU sense
-NCU_INT_PLAIN = {"issue_active_frac": 0.773, "alu_pipe_active_frac": 0.679,
+NCU_INT_PLAIN = {"issue_active_frac": 0.781, "alu_pipe_active_frac": 0.664,
                  "warps_active_frac": 0.375,
                  "source": "ncu smsp__issue_active, sm__pipe_alu_cycles_active, "
                            "sm__warps_active (pct of peak, active cycles) at 300 Mbp"}
