@@ -537,6 +537,14 @@ class beguidedoff:
         return table
 
     # ------------------------------------------------------------------
+    def _chrom_name_array(self) -> np.ndarray:
+        """The chromosome names as an object array (built once)."""
+        arr = getattr(self, "_chrom_names_arr", None)
+        if arr is None or len(arr) != len(self.chrom_names):
+            arr = np.array(list(self.chrom_names) + [None], dtype=object)[:-1]
+            self._chrom_names_arr = arr
+        return arr
+
     def _table_from_records(self, recs, row0, owners, guides, plan_items, return_all,
                             below_by_id):
         """Output table straight from the device epilogue's records: each
@@ -573,7 +581,8 @@ class beguidedoff:
                 arr = self._strand_arrays[st]
                 seq[sel] = extract_windows(arr, pos[sel], 20)
                 pam[sel] = extract_windows(arr, pos[sel] + 20, 6)
-        plen = np.array([len(plan_items[r][1]) for r in row.tolist()], dtype=np.int64)
+        plan_seq = np.array([q for q, _ in plan_items] + [None], dtype=object)[:-1]
+        plen = np.array([len(pm) for _, pm in plan_items], dtype=np.int64)[row]
         gb = _guide_bases([g for g, _ in plan_items])
         weights = np.int64(1) << np.arange(20, dtype=np.int64)
         mmask = ((seq != gb[row]).astype(np.int64) * weights[None, :]).sum(1) if n else \
@@ -611,12 +620,10 @@ class beguidedoff:
         seq_s, pam_s = _decode_strings(seq[idx], pam[idx], plen[idx])
         mpos = _per_unique(mmask[idx], _mismatch_positions)
         cols = {
-            "guide_rna_sequence": np.array([plan_items[r][0] for r in row[idx].tolist()],
-                                           dtype=object),
+            "guide_rna_sequence": plan_seq[row[idx]],
             "base_editor": np.repeat(np.array(editors, dtype=object), sizes),
             "ot_rank": within + 1,
-            "ot_chromosome": np.array([self.chrom_names[c] for c in rep_ci[idx].tolist()],
-                                      dtype=object),
+            "ot_chromosome": self._chrom_name_array()[rep_ci[idx]],
             "ot_position": (rep_local[idx] + 1).astype(np.int64),
             "ot_strand": np.where(slot[idx] == 1, "-", "+").astype(object),
             "ot_sequence": np.array(seq_s, dtype=object),
