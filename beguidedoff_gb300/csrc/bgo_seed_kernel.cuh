@@ -224,7 +224,8 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
                 if (lo >= total) break;
                 const int n_list = min(total - lo, C::kListCap);
                 // list positions [lo, lo + n_list) of the chunk's passing positions
-                if (C::kPasses == 1) {
+                // (one pass, the common case: every lane lists all of its own)
+                if (C::kPasses == 1 || total <= C::kListCap) {
                     int off = off0;
 #pragma unroll
                     for (int u = 0; u < C::kRows; ++u) {
