@@ -178,27 +178,36 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
             const uint32_t win_off = F.three_prime ? 0u : (uint32_t)F.plen;
             const SeedFam &SF = sFam[f - p.fam_begin];
             const int n_tests = SF.n_tests;
-            uint32_t pass[C::kRows];
-            int cnt = 0;
+            uint32_t pass[C::kRows], hw[C::kRows][2], lw[C::kRows][2];
 #pragma unroll
             for (int u = 0; u < C::kRows; ++u) {
                 const int wi = u * 32 + lane;
                 const int rem = lim - 32 * wi;
-                uint32_t ps = rem >= 32 ? 0xFFFFFFFFu : (rem <= 0 ? 0u : (1u << rem) - 1u);
-                const uint32_t h0 = wH[wi], h1 = wH[wi + 1], l0 = wL[wi], l1 = wL[wi + 1];
-                // only the family's own tests run (a loop, not predicated slots)
-#pragma unroll 1
-                for (int k = 0; k < n_tests; ++k) {
-                    const uint32_t sh = SF.pam_shift[k];
-                    const uint4 m = SF.pam_mask[k];
-                    const uint32_t h = sfshr(h0, h1, sh), l = sfshr(l0, l1, sh);
-                    ps &= ((SF.pam_generic >> k) & 1u)
-                              ? (~h & ~l & m.x) | (~h & l & m.y) | (h & ~l & m.z) | (h & l & m.w)
-                              : ~(((h ^ m.x) & m.y) | ((l ^ m.z) & m.w));
-                }
-                pass[u] = ps;
-                cnt += __popc(ps);
+                pass[u] = rem >= 32 ? 0xFFFFFFFFu : (rem <= 0 ? 0u : (1u << rem) - 1u);
+                hw[u][0] = wH[wi];
+                hw[u][1] = wH[wi + 1];
+                lw[u][0] = wL[wi];
+                lw[u][1] = wL[wi + 1];
             }
+            // only the family's own tests run (a loop, not predicated slots),
+            // each test's parameters loaded once for all rows
+#pragma unroll 1
+            for (int k = 0; k < n_tests; ++k) {
+                const uint32_t sh = SF.pam_shift[k];
+                const uint4 m = SF.pam_mask[k];
+                const bool generic = (SF.pam_generic >> k) & 1u;
+#pragma unroll
+                for (int u = 0; u < C::kRows; ++u) {
+                    const uint32_t h = sfshr(hw[u][0], hw[u][1], sh);
+                    const uint32_t l = sfshr(lw[u][0], lw[u][1], sh);
+                    pass[u] &= generic ? (~h & ~l & m.x) | (~h & l & m.y) | (h & ~l & m.z) |
+                                             (h & l & m.w)
+                                       : ~(((h ^ m.x) & m.y) | ((l ^ m.z) & m.w));
+                }
+            }
+            int cnt = 0;
+#pragma unroll
+            for (int u = 0; u < C::kRows; ++u) cnt += __popc(pass[u]);
             int incl = cnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
