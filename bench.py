@@ -38,12 +38,12 @@ sys.path.insert(0, ROOT)
 METRIC = "guide-site comparisons/s"
 UNIT = "cmp/s"
 # DRAM bytes (read + write) of one segment-index scan of the plain workload
-# at 300 Mbp, from ncu (profiles/scan_seed_kernel_ngg100_300mbp.md, capture 13);
+# at 300 Mbp, from ncu (profiles/scan_seed_kernel_ngg100_300mbp.md, capture 15);
 # traffic grows with the genome, so the line scales it to the run's length
-NCU_TRAFFIC_PLAIN = (300_000_000, 225.173248e6 + 3.749376e6)
+NCU_TRAFFIC_PLAIN = (300_000_000, 225.60896e6 + 4.602112e6)
 # the same capture's integer-pipe figures: the kernel is issue-bound, so these
 # are its roofline in the integer-ALU sense
-NCU_INT_PLAIN = {"issue_active_frac": 0.781, "alu_pipe_active_frac": 0.664,
+NCU_INT_PLAIN = {"issue_active_frac": 0.784, "alu_pipe_active_frac": 0.670,
                  "warps_active_frac": 0.375,
                  "source": "ncu smsp__issue_active, sm__pipe_alu_cycles_active, "
                            "sm__warps_active (pct of peak, active cycles) at 300 Mbp"}
