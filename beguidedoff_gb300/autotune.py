@@ -15,8 +15,8 @@ Candidate parameters: scan mode; tile length (positions per warp chunk,
 ``chunk_sites``); guides per mask group (``group_guides``, mode 3); one
 launch per PAM family (``split_families``, mode 2); CTAs per SM the kernel is
 compiled for (``min_blocks``: 3 or 4 CTAs of 256 threads with up to 80 or 64
-registers, or 1 CTA of 768 threads whose 24 warps share one copy of the
-index, mode 2); mismatches tolerated per key region (``tolerance``: 0 with K + 1
+registers, or one CTA whose warps share one copy of the index: 768 threads
+(1) or 512 (2), mode 2); mismatches tolerated per key region (``tolerance``: 0 with K + 1
 regions, or 1 with K / 2 + 1 regions and substitution-expanded buckets,
 mode 2).
 """
@@ -66,6 +66,8 @@ FAMILY_CANDIDATES = (
     ("index/t1/1024/cta768", 0, 1024, 1, 1, 0, 0),
     ("index/t1/i1/cta768", 0, 0, 1, 1, 1, 0),
     ("index/t1/i1/1024/cta768", 0, 1024, 1, 1, 1, 0),
+    ("index/t1/cta512", 0, 0, 2, 1, 0, 0),
+    ("index/t1/1024/cta512", 0, 1024, 2, 1, 0, 0),
 )
 PER_FAMILY_TUNING = (0, 0, 0, 1, 0, 0, 0, 0)
 INDEXED_MAX_K = 7

@@ -410,13 +410,13 @@ static int check_tuning(const bgo_plan *pl, const bgo_tuning *t) {
         (t->group_guides != 0 && t->group_guides != 32 && t->group_guides != 64 &&
          t->group_guides != 128) ||
         t->ctas_per_sm < 0 || t->split_families < 0 || t->split_families > 1 ||
-        (t->min_blocks != 0 && t->min_blocks != 1 && t->min_blocks != 3 && t->min_blocks != 4) ||
+        (t->min_blocks != 0 && (t->min_blocks < 1 || t->min_blocks > 4)) ||
         t->tolerance < 0 ||
         t->tolerance > 1 || t->family_form < 0 || t->family_form > 1 ||
         (t->inline_entries != 0 && t->inline_entries != 1 && t->inline_entries != 2) ||
         t->range_walk < 0 || t->range_walk > 1) {
         set_error("bgo_plan_set_tuning: chunk_sites 1024|2048, group_guides 32|64|128, "
-                  "ctas_per_sm >= 0, split_families 0|1, min_blocks 1|3|4, tolerance 0|1, "
+                  "ctas_per_sm >= 0, split_families 0|1, min_blocks 1-4, tolerance 0|1, "
                   "family_form 0|1, inline_entries 1|2, range_walk 0|1");
         return BGO_ERR_ARG;
     }
@@ -484,18 +484,26 @@ static const bgo_tuning &family_tuning(const bgo_plan *pl, int f) {
 
 // The tuning a segment-index launch over index `sa` runs with: the requested
 // one when the index and the warps' chunk slices fit in shared memory, else
-// the same tolerance and form with 1,024-position chunks, then with 8 warps per
-// CTA, then both.  False when none fits (the family, or the single launch,
-// compares every guide instead).
+// the same tolerance and form with 1,024-position chunks, then with fewer
+// warps per CTA (a 768-thread CTA steps down to 512, then to 256 threads; a
+// 512-thread CTA to 256), each with the requested chunk and then 1,024.  False
+// when none fits (the family, or the single launch, compares every guide
+// instead).
 static bool fitted_seed_tuning(const SeedArgs &sa, const bgo_tuning &t, bgo_tuning &out) {
     const size_t limit = 220 * 1024;
+    const int shapes_768[] = {1, 2, 3}, shapes_512[] = {2, 3}, shapes_256[] = {t.min_blocks};
+    const int *shapes =
+        t.min_blocks == 1 ? shapes_768 : t.min_blocks == 2 ? shapes_512 : shapes_256;
+    const int n_shapes = t.min_blocks == 1 ? 3 : t.min_blocks == 2 ? 2 : 1;
     bgo_tuning c = t;
-    for (int step = 0; step < 4; ++step) {
-        c.chunk_sites = (step & 1) ? 1024 : t.chunk_sites;
-        c.min_blocks = (step & 2) && t.min_blocks == 1 ? 3 : t.min_blocks;
-        if (seed_tuning_smem(sa, c) <= limit) {
-            out = c;
-            return true;
+    for (int i = 0; i < n_shapes; ++i) {
+        for (int half = 0; half < 2; ++half) {
+            c.min_blocks = shapes[i];
+            c.chunk_sites = half ? 1024 : t.chunk_sites;
+            if (seed_tuning_smem(sa, c) <= limit) {
+                out = c;
+                return true;
+            }
         }
     }
     return false;

@@ -57,7 +57,9 @@ size_t seed_smem_bytes(const SeedArgs &sa, int chunk_sites, int warps, bool walk
 // per bucket are compared inline; launch_seed_kernel dispatches the same way.
 size_t seed_tuning_smem(const SeedArgs &sa, const bgo_tuning &t) {
     const int chunk = t.chunk_sites ? t.chunk_sites : 2048;
-    const int warps = t.min_blocks == 1 ? SeedCta<1>::kWarps : SeedCta<3>::kWarps;
+    const int warps = t.min_blocks == 1   ? SeedCta<1>::kWarps
+                      : t.min_blocks == 2 ? SeedCta<2>::kWarps
+                                          : SeedCta<3>::kWarps;
     const bool walk = t.tolerance == 1 || (t.inline_entries != 2 && t.range_walk == 1);
     return seed_smem_bytes(sa, chunk, warps, walk);
 }

@@ -82,16 +82,19 @@ __device__ __noinline__ void finish_candidate(const ScanParams &p, uint32_t m, i
           p.counter);
 }
 
-// CTAs are 256 threads (MINB = 3 or 4 per SM), or one 768-thread CTA per SM
-// (MINB = 1) so that 24 warps share a large index.
+// CTA shapes by MINB: 3 or 4 CTAs of 256 threads per SM; or one CTA per SM
+// whose warps share a large index, of 768 threads (MINB = 1, 24 warps) or 512
+// (MINB = 2, 16 warps, for an index too large to leave room for 24 warps'
+// chunk slices).
 template <int MINB>
 struct SeedCta {
-    static constexpr int kThreads = MINB == 1 ? 768 : kSeedThreads;
+    static constexpr int kThreads = MINB == 1 ? 768 : MINB == 2 ? 512 : kSeedThreads;
     static constexpr int kWarps = kThreads / 32;
+    static constexpr int kPerSm = MINB <= 2 ? 1 : MINB;
 };
 
 template <int K, int TOL, int INLINE, int WALK, int CH, int MINB>
-__global__ void __launch_bounds__(SeedCta<MINB>::kThreads, MINB)
+__global__ void __launch_bounds__(SeedCta<MINB>::kThreads, SeedCta<MINB>::kPerSm)
     scan_seed_kernel(ScanParams p, SeedArgs sa) {
     constexpr int THREADS = SeedCta<MINB>::kThreads;
     constexpr int WARPS = SeedCta<MINB>::kWarps;
@@ -450,6 +453,9 @@ static int launch_form(const ScanParams &p, const SeedArgs &sa, int sm_count, in
     if (min_blocks == 1)
         return c1k ? launch_cm<TOL, INLINE, WALK, 1024, 1>(p, sa, sm_count, ctas_per_sm, s)
                    : launch_cm<TOL, INLINE, WALK, 2048, 1>(p, sa, sm_count, ctas_per_sm, s);
+    if (min_blocks == 2)
+        return c1k ? launch_cm<TOL, INLINE, WALK, 1024, 2>(p, sa, sm_count, ctas_per_sm, s)
+                   : launch_cm<TOL, INLINE, WALK, 2048, 2>(p, sa, sm_count, ctas_per_sm, s);
     return c1k ? launch_cm<TOL, INLINE, WALK, 1024, 3>(p, sa, sm_count, ctas_per_sm, s)
                : launch_cm<TOL, INLINE, WALK, 2048, 3>(p, sa, sm_count, ctas_per_sm, s);
 }

@@ -160,8 +160,11 @@ int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
  *                 family's index in shared memory (higher occupancy when the
  *                 combined index is large), instead of one launch for all
  *   min_blocks    mode 2: CTAs per SM the kernel is compiled for, 3 (up to 80
- *                 registers per thread) or 4 (up to 64) of 256 threads, or 1 of
- *                 768 threads (24 warps sharing one copy of the index); 0 = 3
+ *                 registers per thread) or 4 (up to 64) of 256 threads, or one
+ *                 CTA sharing one copy of the index: 1 = 768 threads (24 warps),
+ *                 2 = 512 threads (16 warps); 0 = 3.  A form that does not fit
+ *                 in shared memory steps down to 1,024-position chunks and to
+ *                 fewer warps
  *   tolerance     mode 2: mismatches allowed in a key region, 0 (K + 1 exact
  *                 regions) or 1 (K / 2 + 1 regions, guides also indexed under
  *                 every single-base substitution of their keys)

@@ -77,14 +77,14 @@ def test_candidate_tunings_are_valid_and_distinct():
         assert t["chunk_sites"] in (0, 1024, 2048), name
         assert t["group_guides"] in (0, 32, 64, 128), name
         assert t["split_families"] in (0, 1) and t["tolerance"] in (0, 1), name
-        assert t["min_blocks"] in (0, 1, 3, 4), name
+        assert t["min_blocks"] in (0, 1, 2, 3, 4), name
         assert t["inline_entries"] in (0, 1, 2) and t["range_walk"] in (0, 1), name
         key = (mode, tuple(t.values()))
         assert key not in seen, name
         seen.add(key)
     fam_seen = set()
     for name, form, chunk, minb, tol, inl, walk in A.FAMILY_CANDIDATES:
-        assert form in (0, 1) and chunk in (0, 1024, 2048) and minb in (0, 1, 3, 4), name
+        assert form in (0, 1) and chunk in (0, 1024, 2048) and minb in (0, 1, 2, 3, 4), name
         assert tol in (0, 1) and inl in (0, 1, 2) and walk in (0, 1), name
         assert (form, chunk, minb, tol, inl, walk) not in fam_seen, name
         fam_seen.add((form, chunk, minb, tol, inl, walk))

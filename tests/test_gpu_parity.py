@@ -204,7 +204,7 @@ def test_indexed_modes_every_k_equal_oracle(k):
                 (0, 0, 0, 0, 0, 0, 2), (1024, 0, 0, 1, 4, 0, 2), (0, 0, 0, 0, 0, 0, 0, 1),
                 (1024, 0, 0, 1, 4, 0, 0, 1), (0, 0, 0, 0, 1, 1), (1024, 0, 0, 1, 1, 1),
                 (0, 0, 0, 0, 1, 0, 0, 1), (2048, 0, 0, 0, 1, 0, 2), (0, 0, 0, 0, 1, 1, 1),
-                (1024, 0, 0, 1, 3, 1, 1)]
+                (1024, 0, 0, 1, 3, 1, 1), (0, 0, 0, 0, 2, 1), (1024, 0, 0, 1, 2, 0, 0, 1)]
         for mode, tune in [(2, t) for t in seed] + [(3, t) for t in tunings]:
             plan.set_tuning(*tune)
             got = f._engine.scan(plan, f._strands, [0, 3], k, mode)
@@ -233,8 +233,9 @@ def test_index_forms_that_outgrow_shared_memory_equal_oracle():
     the keys stay the oracle's in one launch and in per-family launches."""
     genome, rng = _random_genome(91, [300_000, 120_001])
     seqs, pams = [], []
-    # at K = 5 with tolerance 1: NNGRRT fits 768 threads with 1,024-position
-    # chunks, NG 8 warps with 2,048, NRN 8 warps with 1,024, NGG no form
+    # at K = 5 with tolerance 1 the requested 768-thread, 2,048-position form
+    # fits none of these: NNGRRT steps down to 1,024-position chunks, NG to
+    # 512 threads, NRN to 8 warps, and NGG fits no form
     for fam, n in (("NRN", 250), ("NG", 200), ("NGG", 1500), ("NNGRRT", 150)):
         for i in range(n):
             s = "".join(rng.choice(list("ACGT"), 20))
@@ -252,7 +253,8 @@ def test_index_forms_that_outgrow_shared_memory_equal_oracle():
             got = f._engine.scan(plan, f._strands, [0, 3], 5, 2)
             assert np.array_equal(got, exp), tune
         for fam_tune in [dict(tolerance=1, min_blocks=1), dict(min_blocks=1, range_walk=1),
-                         dict(min_blocks=1, inline_entries=2), dict(tolerance=1)]:
+                         dict(min_blocks=1, inline_entries=2), dict(tolerance=1),
+                         dict(tolerance=1, min_blocks=2)]:
             plan.set_tuning(0, 0, 0, 1)
             for fi in range(plan.families().max() + 1):
                 plan.set_family_tuning(fi, **fam_tune)
