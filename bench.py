@@ -767,7 +767,9 @@ def main():
     ap.add_argument("--chunk-sites", type=int, default=0, help="modes 2/3 tile length (0 = default)")
     ap.add_argument("--group-guides", type=int, default=0, help="mode 3 guides per group")
     ap.add_argument("--ctas-per-sm", type=int, default=0)
-    ap.add_argument("--min-blocks", type=int, default=0, help="mode 2: 3 or 4 CTAs of 256 threads per SM; 1 = one of 768, 2 = one of 512")
+    ap.add_argument("--min-blocks", type=int, default=0,
+                    help="mode 2: 3 or 4 CTAs of 256 threads per SM; 1 = one of 768, "
+                         "2 = one of 512")
     ap.add_argument("--tolerance", type=int, default=0, help="mode 2: key-region tolerance 0/1")
     ap.add_argument("--split-families", type=int, default=0, help="mode 2: one launch per family")
     ap.add_argument("--inline-entries", type=int, default=0, help="mode 2: 1 or 2 inline guides")
