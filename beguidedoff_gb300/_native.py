@@ -337,7 +337,8 @@ class Tuning(ctypes.Structure):
                 ("ctas_per_sm", ctypes.c_int32), ("split_families", ctypes.c_int32),
                 ("min_blocks", ctypes.c_int32), ("tolerance", ctypes.c_int32),
                 ("family_form", ctypes.c_int32), ("inline_entries", ctypes.c_int32),
-                ("range_walk", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("range_walk", ctypes.c_int32), ("prefilter", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
 
 class Plan:
@@ -367,22 +368,24 @@ class Plan:
         return {"n_families": nf.value, "n_guides": ng.value}
 
     def set_tuning(self, chunk_sites=0, group_guides=0, ctas_per_sm=0, split_families=0,
-                   min_blocks=0, tolerance=0, inline_entries=0, range_walk=0):
+                   min_blocks=0, tolerance=0, inline_entries=0, range_walk=0, prefilter=0):
         """Launch parameters of scan modes 2 and 3 (see bgo_plan_set_tuning)."""
         t = Tuning(int(chunk_sites), int(group_guides), int(ctas_per_sm), int(split_families),
-                   int(min_blocks), int(tolerance), 0, int(inline_entries), int(range_walk))
+                   int(min_blocks), int(tolerance), 0, int(inline_entries), int(range_walk),
+                   int(prefilter))
         check(lib().bgo_plan_set_tuning(self.handle, ctypes.byref(t)), "bgo_plan_set_tuning")
         self.tuning = {"chunk_sites": int(chunk_sites), "group_guides": int(group_guides),
                        "ctas_per_sm": int(ctas_per_sm), "split_families": int(split_families),
                        "min_blocks": int(min_blocks), "tolerance": int(tolerance),
-                       "inline_entries": int(inline_entries), "range_walk": int(range_walk)}
+                       "inline_entries": int(inline_entries), "range_walk": int(range_walk),
+                       "prefilter": int(prefilter)}
 
     def set_family_tuning(self, family, chunk_sites=0, min_blocks=0, tolerance=0, form=0,
-                          ctas_per_sm=0, inline_entries=0, range_walk=0):
+                          ctas_per_sm=0, inline_entries=0, range_walk=0, prefilter=0):
         """Launch parameters of one PAM family in split launches (form 0:
         segment index, 1: every guide compared)."""
         t = Tuning(int(chunk_sites), 0, int(ctas_per_sm), 1, int(min_blocks), int(tolerance),
-                   int(form), int(inline_entries), int(range_walk))
+                   int(form), int(inline_entries), int(range_walk), int(prefilter))
         check(lib().bgo_plan_set_family_tuning(self.handle, int(family), ctypes.byref(t)),
               "bgo_plan_set_family_tuning")
 

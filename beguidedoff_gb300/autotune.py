@@ -18,7 +18,9 @@ compiled for (``min_blocks``: 3 or 4 CTAs of 256 threads with up to 80 or 64
 registers, or one CTA whose warps share one copy of the index: 768 threads
 (1) or 512 (2), mode 2); mismatches tolerated per key region (``tolerance``: 0 with K + 1
 regions, or 1 with K / 2 + 1 regions and substitution-expanded buckets,
-mode 2).
+mode 2); the prefiltered form (``prefilter``: a lossless byte-table test per
+PAM-passing position in front of the tolerance-1 index, which then stays in
+global memory; all families in one persistent launch unless split).
 """
 from dataclasses import dataclass, field
 from typing import Dict, List, Sequence, Tuple
@@ -46,13 +48,18 @@ CANDIDATES: Tuple[Tuple[str, int, Tuple[int, ...]], ...] = (
     ("segment-index/walk/cta768", 2, (0, 0, 0, 0, 1, 0, 0, 1)),
     ("segment-index/walk/1024/cta768", 2, (1024, 0, 0, 0, 1, 0, 0, 1)),
     ("segment-masks/2048x128", 3, (2048, 128, 0, 0, 0, 0, 0)),
+    ("prefilter", 2, (2048, 0, 0, 0, 0, 1, 0, 0, 1)),
+    ("prefilter/4096", 2, (4096, 0, 0, 0, 0, 1, 0, 0, 1)),
+    ("prefilter/per-family", 2, (2048, 0, 0, 1, 0, 1, 0, 0, 1)),
 )
 TUNING_FIELDS = ("chunk_sites", "group_guides", "ctas_per_sm", "split_families", "min_blocks",
-                 "tolerance", "inline_entries", "range_walk")
+                 "tolerance", "inline_entries", "range_walk", "prefilter")
 # per PAM family, timed on a plan holding that family alone:
 # (name, form (0 segment index, 1 every guide), chunk_sites, min_blocks, tolerance,
-#  inline_entries, range_walk)
+#  inline_entries, range_walk[, prefilter])
 FAMILY_CANDIDATES = (
+    ("prefilter", 0, 2048, 0, 1, 0, 0, 1),
+    ("prefilter/4096", 0, 4096, 0, 1, 0, 0, 1),
     ("every-guide", 1, 0, 0, 0, 0, 0),
     ("index", 0, 0, 0, 0, 0, 0),
     ("index/walk", 0, 0, 0, 0, 0, 1),
@@ -69,7 +76,7 @@ FAMILY_CANDIDATES = (
     ("index/t1/cta512", 0, 0, 2, 1, 0, 0),
     ("index/t1/1024/cta512", 0, 1024, 2, 1, 0, 0),
 )
-PER_FAMILY_TUNING = (0, 0, 0, 1, 0, 0, 0, 0)
+PER_FAMILY_TUNING = (0, 0, 0, 1, 0, 0, 0, 0, 0)
 INDEXED_MAX_K = 7
 
 
@@ -81,7 +88,7 @@ class Choice:
     times_ms: Dict[str, float] = field(default_factory=dict)
     sample_bp: int = 0
     # per-family choice (name "per-family"): PAM -> (name, form, chunk_sites,
-    # min_blocks, tolerance, inline_entries, range_walk, ms alone)
+    # min_blocks, tolerance, inline_entries, range_walk, ms alone, prefilter)
     family: Dict[str, tuple] = field(default_factory=dict)
 
     def as_dict(self):
@@ -106,7 +113,8 @@ class Choice:
             c = self.family.get(pams[row].upper())
             if c is not None:
                 plan.set_family_tuning(f, chunk_sites=c[2], min_blocks=c[3], tolerance=c[4],
-                                       form=c[1], inline_entries=c[5], range_walk=c[6])
+                                       form=c[1], inline_entries=c[5], range_walk=c[6],
+                                       prefilter=c[8] if len(c) > 8 else 0)
 
 
 def signature(pams: Sequence[str], max_mismatches: int) -> tuple:
@@ -210,12 +218,14 @@ class Autotuner:
                                plan.pam_lens[rows], plan.pam_3prime[rows], stream)
             try:
                 best = None
-                for name, form, chunk, minb, tol, inl, walk in FAMILY_CANDIDATES:
-                    sub.set_tuning(chunk, 0, 0, 0, minb, tol, inl, walk)
+                for cand in FAMILY_CANDIDATES:
+                    name, form, chunk, minb, tol, inl, walk = cand[:7]
+                    pf = cand[7] if len(cand) > 7 else 0
+                    sub.set_tuning(chunk, 0, 0, 0, minb, tol, inl, walk, pf)
                     ms = self.engine.scan_time(sub, strands, ne, max_mismatches,
                                                1 if form == 1 else 2, self.reps, stream)
                     if best is None or ms < best[7]:
-                        best = (name, form, chunk, minb, tol, inl, walk, ms)
+                        best = (name, form, chunk, minb, tol, inl, walk, ms, pf)
             finally:
                 sub.close()
             out[pams[int(rows[0])].upper()] = best

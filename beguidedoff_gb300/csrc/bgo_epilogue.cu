@@ -434,12 +434,15 @@ extern "C" int bgo_epilogue_run(bgo_engine *engine, const bgo_plan *plan,
         RowInfo &R = rows[(size_t)inputs[i].plan_row];
         list[(size_t)R.in_end++] = i;
     }
-    unsigned long long n_hits_u = 0;
-    BGO_CUDA(cudaMemcpyAsync(&n_hits_u, engine->d_counter, sizeof(n_hits_u),
-                             cudaMemcpyDeviceToHost, s));
+    unsigned long long cnt[3] = {0, 0, 0};
+    BGO_CUDA(cudaMemcpyAsync(cnt, engine->d_counter, sizeof(cnt), cudaMemcpyDeviceToHost, s));
     BGO_CUDA(cudaStreamSynchronize(s));
-    const int64_t n_hits = (int64_t)n_hits_u;
-    engine->d2h_bytes += 8;
+    const int64_t n_hits = (int64_t)cnt[0];
+    engine->d2h_bytes += (int64_t)sizeof(cnt);
+    if (cnt[2] & 1u) {
+        set_error("bgo_epilogue_run: a chunk copy of the last scan did not complete in time");
+        return BGO_ERR_TIMEOUT;
+    }
     if (n_hits > engine->cap) {
         set_error("bgo_epilogue_run: the last scan overflowed the hit buffer; reserve and rescan");
         return BGO_ERR_STATE;

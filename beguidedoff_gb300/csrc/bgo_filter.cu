@@ -1,0 +1,118 @@
+// Prefiltered segment-index scan (scan mode 2 with tuning.prefilter): the same
+// hits as the segment index, with a cheap lossless test in front of it.
+//
+// Regions.  The tolerance-1 segment index splits the 20 guide positions into
+// S = K / 2 + 1 disjoint regions (SegT<K, 1>).  For a hit the raw mismatch
+// counts d_1..d_S of the regions sum to at most K (the N correction only adds
+// to the raw count, beguidedoff/cuda_search.py:272-308).  If no region is
+// exact, every d_j >= 1 and sum (d_j - 1) <= K - S, so at least M = 2S - K
+// regions have d_j = 1.  Hence every hit with guide g has
+//     some region j with d_j(g) = 0, or
+//     at least M regions with d_j(g) <= 1.
+// A region's key (its first <= 7 bases) differs from the guide's in at most
+// d_j bases, so the same holds with keys in place of regions.
+//
+// Filter tables.  Per PAM family and region, one byte per key (4^7 keys for a
+// region of >= 7 bases): bit 0 is set if some guide's key equals it; bit
+// 1 + (i mod 7) is set if guide i's key is within one substitution of it
+// (its own key included).  For each PAM-passing position the kernel reads the
+// S bytes of its keys and keeps the position iff
+//     (OR of the bytes) has bit 0, or some colour bit is set in >= M bytes
+// (M = 1: any colour bit; M > S: bit 0 only).  Guide g with an exact region
+// sets bit 0; with M regions within one it sets its colour in M bytes: the
+// test never drops a hit.  For 100 NGG guides at K = 4 about 6% of PAM-passing
+// positions survive (bit 0 of the 6-base region alone passes 2.4%).
+//
+// Survivors.  Each kept position (its 20-base window planes, the N bits of
+// the window when its 26-position span holds an N, strand and position) goes
+// into a per-warp queue in shared memory.  Whenever the queue holds a full
+// warp, every lane runs the segment index on one survivor: per region the
+// bucket of the key's single-substitution neighbourhood, then the reference's
+// full compare and N correction (finish_candidate, as in scan_seed_kernel).
+// The index stays in global memory (L1/L2), so shared memory holds only the
+// small filter tables and the warps' chunk slices.
+//
+// Work.  One persistent 768-thread CTA per SM.  Per launch family the warps
+// claim runs of four chunks from a per-family counter (atomicAdd), so the
+// families of a mixed plan share one launch without a tail per family; the
+// CTA loads the next family's filter tables after all its warps are done with
+// the previous one (a CTA barrier per family).  Chunks of 2,048 or 4,096
+// positions are copied into the warp's double buffer by one lane with three
+// 1-D bulk copies (cp.async.bulk, one per plane) completing on an mbarrier;
+// the wait is bounded and reports BGO_ERR_TIMEOUT through the engine.
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "bgo_filter_kernel.cuh"
+
+namespace bgo {
+
+uint32_t filter_tab_bytes(int K) {
+    switch (K) {
+        case 0: return FiltT<0>::kBytesAl;
+        case 1: return FiltT<1>::kBytesAl;
+        case 2: return FiltT<2>::kBytesAl;
+        case 3: return FiltT<3>::kBytesAl;
+        case 4: return FiltT<4>::kBytesAl;
+        case 5: return FiltT<5>::kBytesAl;
+        case 6: return FiltT<6>::kBytesAl;
+        case 7: return FiltT<7>::kBytesAl;
+        default: return 0;
+    }
+}
+
+bool build_filter_tables(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
+                         std::vector<uint8_t> &tables, uint32_t &tab_bytes) {
+    if (K < 0 || K > kSeedMaxK) return false;
+    tab_bytes = filter_tab_bytes(K);
+    tables.assign((size_t)n_fams * tab_bytes, 0);
+    const int S = K / 2 + 1;
+    const int q = kGuideLen / S, r = kGuideLen % S;
+    for (int f = 0; f < n_fams; ++f) {
+        uint8_t *T = tables.data() + (size_t)f * tab_bytes;
+        uint32_t off = 0;
+        for (int j = 0; j < S; ++j) {
+            const int start = j * q + std::min(j, r);
+            const int len = q + (j < r ? 1 : 0);
+            const int kl = std::min(len, kFilterKeyLen);
+            const uint32_t km = (1u << kl) - 1u;
+            for (int i = 0; i < fams[f].gend - fams[f].gbeg; ++i) {
+                const GuideRec &g = recs[fams[f].gbeg + i];
+                const uint8_t colour = (uint8_t)(2u << (i % kFilterColors));
+                const uint32_t hk = (g.h >> start) & km, lk = (g.l >> start) & km;
+                T[off + ((hk << kl) | lk)] |= (uint8_t)(1u | colour);
+                for (int b = 0; b < kl; ++b) {
+                    const uint32_t cur = (((hk >> b) & 1u) << 1) | ((lk >> b) & 1u);
+                    for (uint32_t v = 0; v < 4; ++v) {
+                        if (v == cur) continue;
+                        const uint32_t h2 = (hk & ~(1u << b)) | ((v >> 1) << b);
+                        const uint32_t l2 = (lk & ~(1u << b)) | ((v & 1u) << b);
+                        T[off + ((h2 << kl) | l2)] |= colour;
+                    }
+                }
+            }
+            off += 1u << (2 * kl);
+        }
+        if (off > tab_bytes) return false;
+    }
+    return true;
+}
+
+int launch_filter_4k(const ScanParams &p, const FilterArgs &fa, int sm_count, cudaStream_t s);
+
+int launch_filter_kernel(const ScanParams &p, const FilterArgs &fa, int sm_count, int chunk_sites,
+                         cudaStream_t s) {
+    if (fa.tab_bytes != (int32_t)filter_tab_bytes(p.max_mm)) {
+        set_error("prefiltered segment index: tables built for another max_mismatches");
+        return BGO_ERR_ARG;
+    }
+    if (chunk_sites == 4096) return launch_filter_4k(p, fa, sm_count, s);
+    if (chunk_sites != 2048) {
+        set_error("prefiltered segment index: chunk_sites must be 2048 or 4096");
+        return BGO_ERR_ARG;
+    }
+    return launch_filter_ch<2048>(p, fa, sm_count, s);
+}
+
+}  // namespace bgo

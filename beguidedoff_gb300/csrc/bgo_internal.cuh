@@ -111,6 +111,24 @@ struct SeedArgs {
     int32_t n_fams, n_guides, n_offsets, n_lists;
 };
 
+// Prefiltered segment index (scan mode 2 with tuning.prefilter): per PAM
+// family one byte per key of each tolerance-1 region (first <= kFilterKeyLen
+// bases); the segment index itself stays in global memory.
+constexpr int kFilterKeyLen = 7;
+constexpr int kFilterColors = 7;
+
+struct FilterArgs {
+    const SeedFam *fams;       // the launch's families: fams[f - fam_begin]
+    const uint32_t *offsets;   // segment index (tolerance 1) in global memory
+    const uint2 *entries;
+    const uint16_t *entry_idx;
+    const uint8_t *tables;     // per launch family, tab_bytes each
+    uint32_t *work;            // per launch family: next chunk to claim
+    int *err;                  // bit 0: a chunk copy wait gave up
+    int32_t tab_bytes;
+    int32_t n_fams;
+};
+
 // Segment-mask scan (scan mode 3): the segment index stored as guide bitmasks.
 // Each family is cut into groups of at most kMaskGroupMax guides; for group g,
 // segment j and key code c the table holds the bitmask of the group's guides
@@ -185,13 +203,16 @@ inline int64_t tiles_for(int64_t total_bp) {
 
 // Plane words needed so every tile load [t*256, t*256 + kTileWords) of the
 // plain kernel and every 16-byte-aligned chunk copy of the segment-indexed
-// kernel ([c*64, c*64 + 68) words, see bgo_seed.cu) is inside the buffer.
+// and prefiltered kernels ([c*64, c*64 + 68) words for 2,048-position chunks,
+// [c*128, c*128 + 132) for 4,096) is inside the buffer.
 inline int64_t plane_words_for(int64_t total_bp) {
     int64_t t = tiles_for(total_bp);
     int64_t need = t * (kTileSites / 32) + kTileWords;
     int64_t valid = total_bp - kSiteSpan;
     int64_t chunks = valid > 0 ? ceil_div(valid, 2048) : 0;
     int64_t need2 = chunks * 64 + 68;
+    int64_t chunks4 = valid > 0 ? ceil_div(valid, 4096) : 0;
+    need2 = need2 > chunks4 * 128 + 132 ? need2 : chunks4 * 128 + 132;
     int64_t cover = ceil_div(total_bp > 0 ? total_bp : 1, 32) + 4;
     int64_t w = need > cover ? need : cover;
     w = w > need2 ? w : need2;
@@ -240,6 +261,10 @@ struct bgo_plan {
     // (creation, scans, graph replays); destroy and index rebuilds wait on it
     cudaEvent_t done = nullptr;
     uint64_t index_gen = 0;   // bumped when an index block is replaced
+    // prefilter tables (one block of filter_tab bytes per family) for filter_k
+    int filter_k = -1000;
+    uint32_t filter_tab = 0;
+    unsigned char *d_filter = nullptr;
 };
 
 namespace bgo {
@@ -259,6 +284,13 @@ bool build_mask_index(const FamilyDesc *fams, int n_fams, const GuideRec *recs, 
                       std::vector<MaskGroup> &groups, std::vector<uint32_t> &table,
                       std::vector<uint2> &guides);
 size_t mask_smem_bytes(const MaskArgs &ma);
+// Prefilter tables of families [0, n_fams) for K mismatches (tab_bytes per
+// family); false when K is outside 0..7.
+bool build_filter_tables(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
+                         std::vector<uint8_t> &tables, uint32_t &tab_bytes);
+uint32_t filter_tab_bytes(int K);
+int launch_filter_kernel(const ScanParams &p, const FilterArgs &fa, int sm_count, int chunk_sites,
+                         cudaStream_t s);
 int launch_mask_kernel(const ScanParams &p, const MaskArgs &ma, int sm_count, int ctas_per_sm,
                        cudaStream_t s);
 }  // namespace bgo
@@ -286,4 +318,11 @@ struct bgo_engine {
     int64_t h2d_bytes = 0, d2h_bytes = 0;
     // bumped whenever d_keys / cap change (captured graphs re-capture then)
     uint64_t keys_gen = 0;
+    // per launch family: the prefiltered kernel's next chunk to claim
+    uint32_t *d_work = nullptr;
 };
+// counters of d_counter: hits, pairs evaluated, error flags (bit 0: a chunk
+// copy wait gave up), spare
+constexpr int kEngineCounters = 4;
+// families one prefiltered launch covers (its work counters)
+constexpr int kWorkCap = 4096;

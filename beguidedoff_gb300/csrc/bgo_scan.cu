@@ -225,12 +225,15 @@ extern "C" int bgo_engine_create(int device, bgo_engine **out) {
     if (!e) return BGO_ERR_OOM;
     e->device = device;
     e->cap = 0;
-    cudaError_t ce = cudaMalloc(&e->d_counter, 2 * sizeof(unsigned long long));
-    if (ce == cudaSuccess) ce = cudaMemset(e->d_counter, 0, 2 * sizeof(unsigned long long));
+    cudaError_t ce = cudaMalloc(&e->d_counter, kEngineCounters * sizeof(unsigned long long));
+    if (ce == cudaSuccess)
+        ce = cudaMemset(e->d_counter, 0, kEngineCounters * sizeof(unsigned long long));
+    if (ce == cudaSuccess) ce = cudaMalloc(&e->d_work, kWorkCap * sizeof(uint32_t));
     int sms = 0;
     if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (ce != cudaSuccess) {
         if (e->d_counter) cudaFree(e->d_counter);
+        if (e->d_work) cudaFree(e->d_work);
         delete e;
         return cuda_fail(ce, "bgo_engine_create");
     }
@@ -244,6 +247,7 @@ extern "C" int bgo_engine_destroy(bgo_engine *e) {
     cudaSetDevice(e->device);
     if (e->d_keys) cudaFree(e->d_keys);
     if (e->d_counter) cudaFree(e->d_counter);
+    if (e->d_work) cudaFree(e->d_work);
     if (e->d_epi) cudaFree(e->d_epi);
     if (e->d_epi_rec) cudaFree(e->d_epi_rec);
     if (e->d_epi_out) cudaFree(e->d_epi_out);
@@ -397,6 +401,7 @@ extern "C" int bgo_plan_destroy(bgo_plan *pl) {
     pool_free(pl->device, pl->d_seed);
     pool_free(pl->device, pl->d_seed_fam);
     pool_free(pl->device, pl->d_mask);
+    pool_free(pl->device, pl->d_filter);
     event_give(pl->device, pl->done);
     delete[] pl->h_fams;
     delete[] pl->h_guides;
@@ -406,7 +411,9 @@ extern "C" int bgo_plan_destroy(bgo_plan *pl) {
 
 static int check_tuning(const bgo_plan *pl, const bgo_tuning *t) {
     if (!pl || !t) return BGO_ERR_ARG;
-    if ((t->chunk_sites != 0 && t->chunk_sites != 1024 && t->chunk_sites != 2048) ||
+    if ((t->chunk_sites != 0 && t->chunk_sites != 1024 && t->chunk_sites != 2048 &&
+         !(t->chunk_sites == 4096 && t->prefilter == 1)) ||
+        (t->prefilter == 1 && t->chunk_sites == 1024) || t->prefilter < 0 || t->prefilter > 1 ||
         (t->group_guides != 0 && t->group_guides != 32 && t->group_guides != 64 &&
          t->group_guides != 128) ||
         t->ctas_per_sm < 0 || t->split_families < 0 || t->split_families > 1 ||
@@ -415,9 +422,10 @@ static int check_tuning(const bgo_plan *pl, const bgo_tuning *t) {
         t->tolerance > 1 || t->family_form < 0 || t->family_form > 1 ||
         (t->inline_entries != 0 && t->inline_entries != 1 && t->inline_entries != 2) ||
         t->range_walk < 0 || t->range_walk > 1) {
-        set_error("bgo_plan_set_tuning: chunk_sites 1024|2048, group_guides 32|64|128, "
-                  "ctas_per_sm >= 0, split_families 0|1, min_blocks 1-4, tolerance 0|1, "
-                  "family_form 0|1, inline_entries 1|2, range_walk 0|1");
+        set_error("bgo_plan_set_tuning: chunk_sites 1024|2048 (2048|4096 with prefilter), "
+                  "group_guides 32|64|128, ctas_per_sm >= 0, split_families 0|1, min_blocks 1-4, "
+                  "tolerance 0|1, family_form 0|1, inline_entries 1|2, range_walk 0|1, "
+                  "prefilter 0|1");
         return BGO_ERR_ARG;
     }
     return BGO_OK;
@@ -509,16 +517,22 @@ static bool fitted_seed_tuning(const SeedArgs &sa, const bgo_tuning &t, bgo_tuni
     return false;
 }
 
+// The tolerance a family's index is built with: the prefiltered form always
+// uses tolerance-1 regions.
+static int index_tolerance(const bgo_tuning &t) { return t.prefilter ? 1 : t.tolerance; }
+
 static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s) {
     const bool split = pl->tuning.split_families && pl->n_families > 1;
-    std::vector<int> tols((size_t)pl->n_families, pl->tuning.tolerance);
+    std::vector<int> tols((size_t)pl->n_families, index_tolerance(pl->tuning));
     if (split)
-        for (int f = 0; f < pl->n_families; ++f) tols[(size_t)f] = family_tuning(pl, f).tolerance;
+        for (int f = 0; f < pl->n_families; ++f)
+            tols[(size_t)f] = index_tolerance(family_tuning(pl, f));
     // split launches: a family whose index does not fit in any form compares
     // every guide on its own
     auto applies = [&]() -> int {
         if (!pl->seed_ok) return 0;
         if (split) return 1;
+        if (pl->tuning.prefilter) return 1;  // the index stays in global memory
         for (int v : tols)
             if (v != tols[0]) return 0;  // one launch needs one tolerance
         bgo_tuning fit;
@@ -601,6 +615,30 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
     return applies();
 }
 
+// Builds (once per max_mismatches) and uploads the plan's prefilter tables.
+static int filter_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s) {
+    if (pl->filter_k == K && pl->d_filter) return BGO_OK;
+    if (pl->d_filter) {
+        BGO_CUDA(cudaEventSynchronize(pl->done));  // launches that read the old tables
+        BGO_CUDA(pool_free(pl->device, pl->d_filter));
+        pl->d_filter = nullptr;
+        pl->index_gen++;
+    }
+    std::vector<uint8_t> tabs;
+    uint32_t tab = 0;
+    if (!build_filter_tables(pl->h_fams, pl->n_families, pl->h_guides, K, tabs, tab)) {
+        set_error("prefiltered segment index: max_mismatches outside 0..7");
+        return BGO_ERR_ARG;
+    }
+    BGO_CUDA(pool_alloc(pl->device, (void **)&pl->d_filter, tabs.size() + 16));
+    BGO_CUDA(cudaMemcpyAsync(pl->d_filter, tabs.data(), tabs.size(), cudaMemcpyHostToDevice, s));
+    BGO_CUDA(cudaStreamSynchronize(s));
+    engine->h2d_bytes += (int64_t)tabs.size();
+    pl->filter_k = K;
+    pl->filter_tab = tab;
+    return BGO_OK;
+}
+
 // Builds (once per (max_mismatches, group size)) and uploads the plan's
 // segment-mask index.  Returns 1 when it applies, 0 when the scan must compare
 // every guide (mode 1), or a negative BGO_ERR_*.
@@ -677,7 +715,7 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
     }
     BGO_CUDA(cudaSetDevice(engine->device));
     cudaStream_t s = (cudaStream_t)stream;
-    BGO_CUDA(cudaMemsetAsync(engine->d_counter, 0, 2 * sizeof(unsigned long long), s));
+    BGO_CUDA(cudaMemsetAsync(engine->d_counter, 0, kEngineCounters * sizeof(unsigned long long), s));
     engine->launched = 1;
     if (plan->n_families == 0) return BGO_OK;
     ScanParams p{};
@@ -745,6 +783,41 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
             if (rc == BGO_OK) engine->launches++;
             return rc;
         };
+        // prefiltered form over families [fb, fe): one persistent launch whose
+        // warps claim chunks family by family
+        auto filter_launch = [&](int fb, int fe, const SeedArgs &sa, const bgo_tuning &t) -> int {
+            const int chunk = t.chunk_sites ? t.chunk_sites : 2048;
+            int rc = filter_prepare(engine, mpl, max_mismatches, s);
+            if (rc != BGO_OK) return rc;
+            for (int g0 = fb; g0 < fe; g0 += kWorkCap) {
+                const int g1 = std::min(fe, g0 + kWorkCap);
+                ScanParams q = p;
+                for (int i = 0; i < n_strands; ++i) {
+                    fill_strand(q.strand[i], strands[i], n_encoded[i], i);
+                    q.strand[i].n_tiles = seed_tiles_for(strands[i]->total_bp, chunk);
+                }
+                q.n_strands = n_strands;
+                q.tiles_total = q.strand[0].n_tiles + (n_strands > 1 ? q.strand[1].n_tiles : 0);
+                if (q.tiles_total == 0) return BGO_OK;
+                q.fam_begin = g0;
+                q.fam_end = g1;
+                FilterArgs fa{};
+                fa.fams = sa.fams + (g0 - fb);
+                fa.offsets = sa.offsets;
+                fa.entries = sa.entries;
+                fa.entry_idx = sa.entry_idx;
+                fa.tables = plan->d_filter + (size_t)g0 * plan->filter_tab;
+                fa.work = engine->d_work;
+                fa.err = reinterpret_cast<int *>(engine->d_counter + 2);
+                fa.tab_bytes = (int32_t)plan->filter_tab;
+                fa.n_fams = g1 - g0;
+                BGO_CUDA(cudaMemsetAsync(engine->d_work, 0, sizeof(uint32_t) * (size_t)(g1 - g0), s));
+                rc = launch_filter_kernel(q, fa, engine->sm_count, chunk, s);
+                if (rc != BGO_OK) return rc;
+                engine->launches++;
+            }
+            return BGO_OK;
+        };
         auto every_guide_launch = [&](int fb, int fe) -> int {
             ScanParams q = p;
             for (int i = 0; i < n_strands; ++i) fill_strand(q.strand[i], strands[i], n_encoded[i], i);
@@ -762,13 +835,18 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
         if (plan->tuning.split_families && plan->n_families > 1) {
             for (int f = 0; f < plan->n_families; ++f) {
                 const SeedArgs &sa = plan->seed_fam[(size_t)f];
+                const bgo_tuning &ft = family_tuning(plan, f);
                 bgo_tuning fit;
-                const int rc = family_tuning(plan, f).family_form == 0 &&
-                                       fitted_seed_tuning(sa, family_tuning(plan, f), fit)
+                const int rc = ft.family_form == 0 && ft.prefilter
+                                   ? filter_launch(f, f + 1, sa, ft)
+                               : ft.family_form == 0 && fitted_seed_tuning(sa, ft, fit)
                                    ? seed_launch(f, f + 1, sa, fit)
                                    : every_guide_launch(f, f + 1);
                 if (rc != BGO_OK) return rc;
             }
+        } else if (plan->tuning.prefilter) {
+            const int rc = filter_launch(0, plan->n_families, plan->seed, plan->tuning);
+            if (rc != BGO_OK) return rc;
         } else {
             bgo_tuning fit;
             fitted_seed_tuning(plan->seed, plan->tuning, fit);  // applies() checked it fits
@@ -959,11 +1037,16 @@ extern "C" int bgo_scan_collect(bgo_engine *engine, uint64_t *keys, int64_t capa
     }
     BGO_CUDA(cudaSetDevice(engine->device));
     cudaStream_t s = (cudaStream_t)stream;
-    unsigned long long n = 0;
-    BGO_CUDA(cudaMemcpyAsync(&n, engine->d_counter, sizeof(n), cudaMemcpyDeviceToHost, s));
+    unsigned long long cnt[3] = {0, 0, 0};
+    BGO_CUDA(cudaMemcpyAsync(cnt, engine->d_counter, sizeof(cnt), cudaMemcpyDeviceToHost, s));
     BGO_CUDA(cudaStreamSynchronize(s));
+    engine->d2h_bytes += (int64_t)sizeof(cnt);
+    if (cnt[2] & 1u) {
+        set_error("bgo_scan_collect: a chunk copy of the last scan did not complete in time");
+        return BGO_ERR_TIMEOUT;
+    }
+    const unsigned long long n = cnt[0];
     *n_hits = (int64_t)n;
-    engine->d2h_bytes += (int64_t)sizeof(n);
     if (keys && (int64_t)n <= capacity && (int64_t)n <= engine->cap && n > 0) {
         BGO_CUDA(cudaMemcpyAsync(keys, engine->d_keys, (size_t)n * sizeof(uint64_t),
                                  cudaMemcpyDeviceToHost, s));

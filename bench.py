@@ -368,7 +368,8 @@ def bench_ours(args, ws, rank, local):
     t0 = time.perf_counter()
     # a fixed mode runs every search() with the command line's launch tuning
     tuning = (args.chunk_sites, args.group_guides, args.ctas_per_sm, args.split_families,
-              args.min_blocks, args.tolerance, args.inline_entries, args.range_walk)
+              args.min_blocks, args.tolerance, args.inline_entries, args.range_walk,
+              args.prefilter)
     f = beguidedoff(None, max_mismatches=args.max_mm, genome_data=genome,
                     device=f"cuda:{local}", scan_mode=args.mode,
                     scan_tuning=None if args.mode == "auto" else tuning)
@@ -774,6 +775,8 @@ def main():
     ap.add_argument("--split-families", type=int, default=0, help="mode 2: one launch per family")
     ap.add_argument("--inline-entries", type=int, default=0, help="mode 2: 1 or 2 inline guides")
     ap.add_argument("--range-walk", type=int, default=0, help="mode 2: per-lane walk of buckets")
+    ap.add_argument("--prefilter", type=int, default=0,
+                    help="mode 2: the prefiltered form (tolerance 1; chunk sites 2048|4096)")
     ap.add_argument("--genome-bp", type=int, default=3_100_000_000)
     ap.add_argument("--guides", type=int, default=100)
     ap.add_argument("--max-mm", type=int, default=4)

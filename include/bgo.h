@@ -152,6 +152,7 @@ int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
  * Launch parameters of a plan (scan modes 2 and 3), normally chosen by the
  * autotuner (beguidedoff_gb300/autotune.py).  Zero fields keep the defaults.
  *   chunk_sites   modes 2/3: positions per warp chunk ("tile length"): 1024 or 2048
+ *                 (4096 with prefilter)
  *   group_guides  mode 3: guides per mask group ("guides per block"): 32, 64
  *                 or 128; a family larger than this is cut into several groups
  *   ctas_per_sm   cap on resident CTAs per SM for the grid size (0 = the
@@ -174,6 +175,16 @@ int bgo_scan_stats(bgo_engine *engine, int64_t *pairs_evaluated, void *stream);
  *   range_walk    mode 2, tolerance 0 with one inline guide: the rest of a
  *                 bucket walked by its own lane (1) instead of spread over the
  *                 warp (0); tolerance 1 always walks
+ *   prefilter     mode 2: 1 = the prefiltered form: per PAM-passing position a
+ *                 lossless test on one byte per tolerance-1 region key
+ *                 (shared memory) keeps the few positions that can hold a hit,
+ *                 which then go through the tolerance-1 segment index in
+ *                 global memory; chunks staged by 1-D bulk copies; one
+ *                 persistent CTA per SM whose warps claim chunks of each
+ *                 family from a counter (all families in one launch unless
+ *                 split_families).  chunk_sites 2048 (default) or 4096;
+ *                 min_blocks, inline_entries and range_walk do not apply, and
+ *                 the index is always built with tolerance 1
  * Changing group_guides rebuilds the mask index at the next launch.  No
  * reference counterpart: the reference fixes 256 threads x 200 Mbp chunks.
  */
@@ -187,7 +198,8 @@ typedef struct bgo_tuning {
     int32_t family_form;   /* per-family tuning only: 0 segment index, 1 compare every guide */
     int32_t inline_entries;
     int32_t range_walk;
-    int32_t reserved[3];
+    int32_t prefilter;
+    int32_t reserved[2];
 } bgo_tuning;
 int bgo_plan_set_tuning(bgo_plan *plan, const bgo_tuning *tuning);
 

@@ -74,7 +74,10 @@ def test_candidate_tunings_are_valid_and_distinct():
     for name, mode, tune in A.CANDIDATES:
         t = dict(zip(A.TUNING_FIELDS, tuple(tune) + (0,) * (len(A.TUNING_FIELDS) - len(tune))))
         assert mode in (1, 2, 3), name
-        assert t["chunk_sites"] in (0, 1024, 2048), name
+        assert t["chunk_sites"] in (0, 1024, 2048) or (
+            t["chunk_sites"] == 4096 and t["prefilter"] == 1), name
+        assert t["prefilter"] in (0, 1), name
+        assert not (t["prefilter"] and (t["tolerance"] != 1 or t["chunk_sites"] == 1024)), name
         assert t["group_guides"] in (0, 32, 64, 128), name
         assert t["split_families"] in (0, 1) and t["tolerance"] in (0, 1), name
         assert t["min_blocks"] in (0, 1, 2, 3, 4), name
@@ -83,11 +86,15 @@ def test_candidate_tunings_are_valid_and_distinct():
         assert key not in seen, name
         seen.add(key)
     fam_seen = set()
-    for name, form, chunk, minb, tol, inl, walk in A.FAMILY_CANDIDATES:
-        assert form in (0, 1) and chunk in (0, 1024, 2048) and minb in (0, 1, 2, 3, 4), name
-        assert tol in (0, 1) and inl in (0, 1, 2) and walk in (0, 1), name
-        assert (form, chunk, minb, tol, inl, walk) not in fam_seen, name
-        fam_seen.add((form, chunk, minb, tol, inl, walk))
+    for cand in A.FAMILY_CANDIDATES:
+        name, form, chunk, minb, tol, inl, walk = cand[:7]
+        pf = cand[7] if len(cand) > 7 else 0
+        assert form in (0, 1) and minb in (0, 1, 2, 3, 4), name
+        assert chunk in (0, 1024, 2048) or (chunk == 4096 and pf == 1), name
+        assert tol in (0, 1) and inl in (0, 1, 2) and walk in (0, 1) and pf in (0, 1), name
+        assert not (pf and (tol != 1 or chunk == 1024)), name
+        assert (form, chunk, minb, tol, inl, walk, pf) not in fam_seen, name
+        fam_seen.add((form, chunk, minb, tol, inl, walk, pf))
 
 
 def test_per_family_choice_applies_each_familys_form():
@@ -114,6 +121,6 @@ def test_per_family_choice_applies_each_familys_form():
     ch.apply(plan, ["NGG", "NRN", "ngg", "NNGRRT", "NG"])
     assert plan.tunings[-1] == A.PER_FAMILY_TUNING
     assert plan.fam_calls[0] == dict(chunk_sites=0, min_blocks=1, tolerance=1, form=0,
-                                     inline_entries=0, range_walk=0)
+                                     inline_entries=0, range_walk=0, prefilter=0)
     assert plan.fam_calls[1]["form"] == 1
     assert 2 not in plan.fam_calls

@@ -204,7 +204,11 @@ def test_indexed_modes_every_k_equal_oracle(k):
                 (0, 0, 0, 0, 0, 0, 2), (1024, 0, 0, 1, 4, 0, 2), (0, 0, 0, 0, 0, 0, 0, 1),
                 (1024, 0, 0, 1, 4, 0, 0, 1), (0, 0, 0, 0, 1, 1), (1024, 0, 0, 1, 1, 1),
                 (0, 0, 0, 0, 1, 0, 0, 1), (2048, 0, 0, 0, 1, 0, 2), (0, 0, 0, 0, 1, 1, 1),
-                (1024, 0, 0, 1, 3, 1, 1), (0, 0, 0, 0, 2, 1), (1024, 0, 0, 1, 2, 0, 0, 1)]
+                (1024, 0, 0, 1, 3, 1, 1), (0, 0, 0, 0, 2, 1), (1024, 0, 0, 1, 2, 0, 0, 1),
+                # prefiltered form: 2,048 and 4,096 positions, all families in one
+                # launch or one launch per family
+                (0, 0, 0, 0, 0, 1, 0, 0, 1), (4096, 0, 0, 0, 0, 1, 0, 0, 1),
+                (2048, 0, 0, 1, 0, 1, 0, 0, 1)]
         for mode, tune in [(2, t) for t in seed] + [(3, t) for t in tunings]:
             plan.set_tuning(*tune)
             got = f._engine.scan(plan, f._strands, [0, 3], k, mode)
@@ -216,11 +220,52 @@ def test_indexed_modes_every_k_equal_oracle(k):
         forms = [dict(form=1), dict(tolerance=1, chunk_sites=1024), dict(min_blocks=4),
                  dict(tolerance=1, min_blocks=4), dict(chunk_sites=1024, inline_entries=2),
                  dict(tolerance=1, min_blocks=1), dict(min_blocks=1, range_walk=1),
-                 dict(tolerance=1, inline_entries=1, chunk_sites=1024, min_blocks=1)]
+                 dict(tolerance=1, inline_entries=1, chunk_sites=1024, min_blocks=1),
+                 dict(tolerance=1, prefilter=1), dict(tolerance=1, prefilter=1, chunk_sites=4096)]
         for fi in range(fam.max() + 1):
             plan.set_family_tuning(fi, **forms[fi % len(forms)])
         got = f._engine.scan(plan, f._strands, [0, 3], k, 2)
         assert np.array_equal(got, exp), "per-family"
+        plan.close()
+    finally:
+        f.close()
+
+
+@pytest.mark.parametrize("k,chunk", [(4, 2048), (4, 4096), (2, 2048), (3, 4096)])
+def test_prefilter_headline_shape_equals_oracle(k, chunk):
+    """The prefiltered form on the headline's shape: 100 NGG guides, many
+    planted sites per guide (survivor queues fill, flush mid-chunk and carry
+    over between chunks), N blocks, a short chromosome and junction
+    straddlers; keys equal the oracle's, and a graph replay equals the plain
+    launch."""
+    genome, rng = _random_genome(500 + k, [1_500_000, 61, 1_100_003, 400_000])
+    seqs = ["".join(rng.choice(list("ACGT"), 20)) for _ in range(100)]
+    for s in seqs:
+        _plant(genome, rng, s, "NGG", 12, k)
+    pams = ["NGG"] * len(seqs)
+    exp = oracle_keys(genome, seqs, pams, k)
+    assert exp.size > 500
+    f = beguidedoff(None, max_mismatches=k, genome_data=genome)
+    try:
+        plan = f._plan(seqs, pams)
+        plan.set_tuning(chunk, 0, 0, 0, 0, 1, 0, 0, 1)
+        got = f._engine.scan(plan, f._strands, [0, 3], k, 2)
+        assert got.size == exp.size and np.array_equal(got, exp)
+        # the index is consulted only for survivors: far fewer pairs than
+        # the index alone evaluates
+        pf_pairs = f._engine.pairs_evaluated()
+        plan.set_tuning(chunk if chunk == 2048 else 0, 0, 0, 0, 1, 1)
+        assert np.array_equal(f._engine.scan(plan, f._strands, [0, 3], k, 2), exp)
+        assert pf_pairs < f._engine.pairs_evaluated()
+        plan.set_tuning(chunk, 0, 0, 0, 0, 1, 0, 0, 1)
+        g = _native.Graph(f._engine, plan, f._strands, [0, 3], k, 2)
+        try:
+            for _ in range(2):
+                g.replay()
+                n, keys = f._engine.collect()
+                assert n == exp.size and np.array_equal(keys, exp)
+        finally:
+            g.close()
         plan.close()
     finally:
         f.close()
