@@ -29,17 +29,30 @@
 // warp, every lane runs the segment index on one survivor: per region the
 // bucket of the key's single-substitution neighbourhood, then the reference's
 // full compare and N correction (finish_candidate, as in scan_seed_kernel).
-// The index stays in global memory (L1/L2), so shared memory holds only the
-// small filter tables and the warps' chunk slices.
+// Each lane tests two list positions per round, and a lane without a survivor
+// stores into a spare queue slot, so the round has no per-lane branch.
+//
+// Survivor index.  When the largest launch family's index fits beside the
+// tables and slices, and its descriptors fit 16 bits (entry starts < 4,096,
+// bucket counts < 16), the CTA copies each family's descriptors, the
+// family-local guide index of every entry (2 bytes) and the family's guide
+// planes (8 bytes per guide) into shared memory at the family's start; else
+// survivors read the index (with full guide planes per entry) from global
+// memory (L1/L2).
 //
 // Work.  One persistent 768-thread CTA per SM.  Per launch family the warps
-// claim runs of four chunks from a per-family counter (atomicAdd), so the
+// take the first three quarters of the chunks in a static grid stride and
+// claim the rest in runs of two from a per-family counter (atomicAdd), so the
 // families of a mixed plan share one launch without a tail per family; the
 // CTA loads the next family's filter tables after all its warps are done with
 // the previous one (a CTA barrier per family).  Chunks of 2,048 or 4,096
 // positions are copied into the warp's double buffer by one lane with three
 // 1-D bulk copies (cp.async.bulk, one per plane) completing on an mbarrier;
 // the wait is bounded and reports BGO_ERR_TIMEOUT through the engine.
+//
+// This translation unit instantiates the 2,048-position form with the index
+// in shared memory; bgo_filter_2k_g.cu, bgo_filter_4k.cu and bgo_filter_4k_s.cu
+// the other forms.
 #include <cuda_runtime.h>
 
 #include <vector>
@@ -99,7 +112,16 @@ bool build_filter_tables(const FamilyDesc *fams, int n_fams, const GuideRec *rec
     return true;
 }
 
-int launch_filter_4k(const ScanParams &p, const FilterArgs &fa, int sm_count, cudaStream_t s);
+size_t filter_smem_fixed_bytes(int K, int chunk_sites) {
+    const size_t per = (sizeof(SeedFam) + 15) / 16 * 16 +
+                       (size_t)kFilterWarps * (chunk_sites == 4096 ? FiltChunk<4096>::kSlice
+                                                                   : FiltChunk<2048>::kSlice);
+    return filter_tab_bytes(K) + per;
+}
+
+int launch_filter_2k_g(const ScanParams &p, const FilterArgs &fa, int sm_count, cudaStream_t s);
+int launch_filter_4k_g(const ScanParams &p, const FilterArgs &fa, int sm_count, cudaStream_t s);
+int launch_filter_4k_s(const ScanParams &p, const FilterArgs &fa, int sm_count, cudaStream_t s);
 
 int launch_filter_kernel(const ScanParams &p, const FilterArgs &fa, int sm_count, int chunk_sites,
                          cudaStream_t s) {
@@ -107,12 +129,21 @@ int launch_filter_kernel(const ScanParams &p, const FilterArgs &fa, int sm_count
         set_error("prefiltered segment index: tables built for another max_mismatches");
         return BGO_ERR_ARG;
     }
-    if (chunk_sites == 4096) return launch_filter_4k(p, fa, sm_count, s);
-    if (chunk_sites != 2048) {
+    if (chunk_sites != 2048 && chunk_sites != 4096) {
         set_error("prefiltered segment index: chunk_sites must be 2048 or 4096");
         return BGO_ERR_ARG;
     }
-    return launch_filter_ch<2048>(p, fa, sm_count, s);
+    if (fa.idx_smem_bytes < 0 || fa.idx_smem_bytes % 16 ||
+        filter_smem_fixed_bytes(p.max_mm, chunk_sites) + (size_t)fa.idx_smem_bytes >
+            (size_t)kFilterSmemLimit) {
+        set_error("prefiltered segment index: the index does not fit in shared memory");
+        return BGO_ERR_ARG;
+    }
+    const bool ism = fa.idx_smem_bytes > 0;
+    if (chunk_sites == 4096)
+        return ism ? launch_filter_4k_s(p, fa, sm_count, s) : launch_filter_4k_g(p, fa, sm_count, s);
+    return ism ? launch_filter_ch<2048, 1>(p, fa, sm_count, s)
+               : launch_filter_2k_g(p, fa, sm_count, s);
 }
 
 }  // namespace bgo

@@ -1,8 +1,9 @@
 // Prefiltered segment-index scan kernel (scan mode 2 with tuning.prefilter),
-// included by the translation units that instantiate its chunk lengths
-// (bgo_filter.cu: 2,048 positions, bgo_filter_4k.cu: 4,096) so that they
-// compile in parallel.  The algorithm and its exactness argument are at the
-// top of bgo_filter.cu.
+// included by the translation units that instantiate its forms (chunk length
+// 2,048 or 4,096 positions, survivor index in shared or global memory:
+// bgo_filter.cu, bgo_filter_2k_g.cu, bgo_filter_4k.cu, bgo_filter_4k_s.cu) so
+// that they compile in parallel.  The algorithm and its exactness argument are
+// at the top of bgo_filter.cu.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -14,12 +15,27 @@
 
 namespace bgo {
 
-constexpr int kFilterThreads = 768;  // one CTA per SM, 24 warps
+#ifndef BGO_FILTER_THREADS
+#define BGO_FILTER_THREADS 768
+#endif
+constexpr int kFilterThreads = BGO_FILTER_THREADS;  // one CTA per SM
 constexpr int kFilterWarps = kFilterThreads / 32;
 constexpr int kSurvCap = 64;         // per-warp survivor queue (two rounds)
-constexpr int kClaimChunks = 4;      // chunks per work claim
+constexpr int kClaimChunks = 2;      // chunks per work claim
+#ifndef BGO_FILTER_STATIC_QUARTERS
+#define BGO_FILTER_STATIC_QUARTERS 3
+#endif
+// quarters of a family's chunks handed out in a static grid stride
+constexpr int kStaticQuarters = BGO_FILTER_STATIC_QUARTERS;
+#ifndef BGO_FILTER_PER
+#define BGO_FILTER_PER 2
+#endif
+// list positions per lane in one filter round
+constexpr int kFilterPer = BGO_FILTER_PER;
 // a bounded wait on a chunk copy gives up after this many nanoseconds
 constexpr unsigned long long kCopyWaitNs = 2000000000ull;
+// dynamic shared memory a prefiltered form may take
+constexpr int kFilterSmemLimit = 227 * 1024;
 
 // Filter regions: the tolerance-1 regions SegT<K, 1> of the segment index,
 // keyed by their first <= kFilterKeyLen bases; region j's table of one byte
@@ -44,26 +60,29 @@ struct FiltT {
 
 // Per-warp shared-memory slice for chunks of CH positions: two chunk buffers
 // (H, L, N planes, each CH/32 + 4 words), the compacted list of PAM-passing
-// positions, the survivor queue and the two chunk buffers' mbarriers.
+// positions, the survivor queue (plus one slot that absorbs the stores of
+// lanes without a survivor) and the two chunk buffers' mbarriers.
 template <int CH>
 struct FiltChunk {
     static constexpr int kRows = CH / 1024;     // 32-position words per lane
     static constexpr int kWords = CH / 32 + 4;  // + halo, a multiple of 4 words
     static constexpr uint32_t kPlaneBytes = kWords * 4u;
     static constexpr size_t kBuf = 3 * (size_t)kPlaneBytes;
-    static constexpr int kListCap = 1024;
+    static constexpr int kListCap = CH >= 4096 ? 512 : 1024;
     static constexpr int kPasses = CH / kListCap;
     static constexpr size_t kListOff = 2 * kBuf;
     static constexpr size_t kQueueOff = kListOff + kListCap * sizeof(uint16_t);
-    static constexpr size_t kBarOff = kQueueOff + kSurvCap * sizeof(uint4);
+    static constexpr size_t kBarOff = kQueueOff + (kSurvCap + 1) * sizeof(uint4);
     static constexpr size_t kSlice = kBarOff + 16;
     static_assert(kPlaneBytes % 16 == 0, "bulk copies are whole 16-byte units");
     static_assert(kBuf % 16 == 0 && kQueueOff % 16 == 0 && kSlice % 16 == 0,
                   "slice parts stay 16-byte aligned");
 };
 
+// Dynamic shared memory of a form besides the survivor index: filter tables,
+// the family's SeedFam and the warps' slices.
 template <int K, int CH>
-constexpr size_t filter_smem_bytes() {
+constexpr size_t filter_smem_fixed() {
     return FiltT<K>::kBytesAl + (sizeof(SeedFam) + 15) / 16 * 16 +
            (size_t)kFilterWarps * FiltChunk<CH>::kSlice;
 }
@@ -128,14 +147,32 @@ __device__ __forceinline__ uint32_t at_least_two(const uint32_t (&x)[S]) {
     }
 }
 
+// The survivor rounds' view of a family's index, held in registers: region
+// j's descriptors start at seg_off[j] and its entries at seg_ent[j]; in the
+// shared-memory form also the descriptor, entry-index and guide-plane arrays.
+template <int K>
+struct FiltView {
+    uint32_t seg_off[SegT<K, 1>::S], seg_ent[SegT<K, 1>::S];
+    uint32_t gbeg;  // first row of the family in the family-sorted guide table
+    const uint16_t *off16;
+    const uint16_t *idx16;
+    const uint2 *gpl;
+};
+
 // Survivor record: x = h20 | strand index << 31, y = l20, z = N bits of the
 // guide window (0 without an N in the 26-position span), w = position.
-// The full segment-index check of one survivor per lane (`valid` lanes).
-template <int K>
-__device__ __forceinline__ void filter_heavy(const ScanParams &p, const FilterArgs &fa, uint4 r,
-                                             bool valid, const uint32_t (&seg_off)[SegT<K, 1>::S],
-                                             const uint32_t (&seg_ent)[SegT<K, 1>::S],
-                                             uint32_t gbeg, uint32_t &cand) {
+// The full segment-index check of one survivor per lane (`valid` lanes): per
+// region the bucket of the key's single-substitution neighbourhood, then
+// every entry's full compare and the N correction (finish_candidate, as in
+// scan_seed_kernel).  The index is read from shared memory (ISM: fv holds the
+// family's 16-bit descriptors, entry start | count << 12, then the
+// family-local guide index of each entry, then the family's guide planes) or
+// from global memory (32-bit descriptors, entry start | count << 16, entries
+// with their guide planes, entry guide indices).  Returns the entries
+// compared.
+template <int K, int ISM>
+__device__ __forceinline__ uint32_t filter_heavy(const ScanParams &p, const FilterArgs &fa,
+                                                 const FiltView<K> &fv, uint4 r, bool valid) {
     using G = SegT<K, 1>;
     constexpr int S = G::S;
     const uint32_t h20 = r.x & 0xFFFFFu, l20 = r.y;
@@ -143,26 +180,47 @@ __device__ __forceinline__ void filter_heavy(const ScanParams &p, const FilterAr
     const uint32_t ne = (uint32_t)(si ? p.strand[1].n_encoded : p.strand[0].n_encoded);
     const uint64_t slot = (uint64_t)(si ? p.strand[1].slot : p.strand[0].slot);
     const uint64_t pos = (uint64_t)r.w;
+    const uint16_t *off16 = fv.off16;
+    const uint16_t *idx16 = fv.idx16;
+    const uint2 *gpl = fv.gpl;
+    uint32_t cand = 0;
 #pragma unroll
     for (int j = 0; j < S; ++j) {
         const int st = G::start(j), kl = G::klen(j);
         const uint32_t km = (1u << kl) - 1u;
         const uint32_t code = (((h20 >> st) & km) << kl) | ((l20 >> st) & km);
-        const uint32_t d = valid ? __ldg(fa.offsets + seg_off[j] + code) : 0u;
-        const uint32_t nn = d >> 16, e0 = seg_ent[j] + (d & 0xFFFFu);
+        uint32_t nn, e0;
+        if (ISM) {
+            const uint32_t d = valid ? off16[fv.seg_off[j] + code] : 0u;
+            nn = d >> 12;
+            e0 = fv.seg_ent[j] + (d & 0xFFFu);
+        } else {
+            const uint32_t d = valid ? __ldg(fa.offsets + fv.seg_off[j] + code) : 0u;
+            nn = d >> 16;
+            e0 = fv.seg_ent[j] + (d & 0xFFFFu);
+        }
         cand += nn;
         for (uint32_t i = 0; i < nn; ++i) {
-            const uint2 e = __ldg(fa.entries + e0 + i);
+            uint2 e;
+            uint32_t gi = 0;
+            if (ISM) {
+                gi = idx16[e0 + i];
+                e = gpl[gi];
+            } else {
+                e = __ldg(fa.entries + e0 + i);
+            }
             const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
             const int cm = __popc(m);
-            if (cm <= K)
-                finish_candidate<K, 1>(p, m, cm, e, __ldg(fa.entry_idx + e0 + i), j, r.z, ne,
-                                       slot, pos, gbeg);
+            if (cm <= K) {
+                if (!ISM) gi = __ldg(fa.entry_idx + e0 + i);
+                finish_candidate<K, 1>(p, m, cm, e, gi, j, r.z, ne, slot, pos, fv.gbeg);
+            }
         }
     }
+    return cand;
 }
 
-template <int K, int CH>
+template <int K, int CH, int ISM>
 __global__ void __launch_bounds__(kFilterThreads, 1)
     scan_filter_kernel(ScanParams p, FilterArgs fa) {
     using FT = FiltT<K>;
@@ -172,12 +230,14 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
     extern __shared__ __align__(128) unsigned char smem[];
     uint8_t *sTab = smem;
     SeedFam *sSF = reinterpret_cast<SeedFam *>(smem + FT::kBytesAl);
-    unsigned char *slices = smem + FT::kBytesAl + (sizeof(SeedFam) + 15) / 16 * 16;
+    unsigned char *sIdxBlk = smem + FT::kBytesAl + (sizeof(SeedFam) + 15) / 16 * 16;
+    unsigned char *slices = sIdxBlk + (ISM ? fa.idx_smem_bytes : 0);
     __shared__ unsigned long long sCand;
 
     const int t = threadIdx.x;
     const int lane = t & 31;
     const int warp = t >> 5;
+    const uint32_t lt_mask = (1u << lane) - 1u;
     unsigned char *slice = slices + warp * C::kSlice;
     uint16_t *wList = reinterpret_cast<uint16_t *>(slice + C::kListOff);
     uint4 *wQ = reinterpret_cast<uint4 *>(slice + C::kQueueOff);
@@ -192,15 +252,16 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
     }
     __syncwarp();
 
-    const int64_t chunks0 = p.strand[0].n_tiles;
-    const int64_t n_chunks = p.tiles_total;
+    // chunk indices fit 32 bits (the host checks tiles_total < 2^31)
+    const int chunks0 = (int)p.strand[0].n_tiles;
+    const int n_chunks = (int)p.tiles_total;
     // Copies chunk c's words [c*CH/32, c*CH/32 + kWords) of the three planes
     // into buffer b (the planes are padded so that the copy never leaves them,
     // and zero beyond total_bp).  One lane issues the three bulk copies.
-    auto issue = [&](int64_t c, int b) {
+    auto issue = [&](int c, int b) {
         if (lane == 0) {
             const bool second = c >= chunks0;
-            const int64_t w0 = (second ? c - chunks0 : c) * (CH / 32);
+            const int64_t w0 = (int64_t)(second ? c - chunks0 : c) * (CH / 32);
             const StrandDesc &sd = second ? p.strand[1] : p.strand[0];
             const uint32_t dst = buf0 + (uint32_t)(b * C::kBuf);
             const uint32_t bar = bar0 + 8u * (uint32_t)b;
@@ -213,10 +274,23 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
             bulk_g2s(dst + 2u * C::kPlaneBytes, sd.N + w0, C::kPlaneBytes, bar);
         }
     };
-    auto claim = [&](int fi) -> int64_t {
+    // Chunk order of a warp: the first kStaticQuarters/4 of the chunks in a
+    // static grid stride over all warps (no atomics), the rest claimed in runs
+    // of kClaimChunks from the family's counter, so that warps that finish
+    // early take the tail.
+    const int n_warps = (int)gridDim.x * kFilterWarps;
+    const int gwarp = (int)blockIdx.x * kFilterWarps + warp;
+    const int static_rounds = (int)((int64_t)n_chunks * kStaticQuarters / 4 / n_warps);
+    const int dyn0 = static_rounds * n_warps;
+    int round = 0, run = 0, run_end = 0;
+    auto next_chunk = [&](int fi) -> int {
+        if (round < static_rounds) return gwarp + (round++) * n_warps;
+        if (run < run_end) return run++;
         uint32_t c = 0;
         if (lane == 0) c = atomicAdd(fa.work + fi, (uint32_t)kClaimChunks);
-        return (int64_t)__shfl_sync(0xFFFFFFFFu, c, 0);
+        run = dyn0 + (int)__shfl_sync(0xFFFFFFFFu, c, 0);
+        run_end = run + kClaimChunks < n_chunks ? run + kClaimChunks : n_chunks;
+        return run < n_chunks ? run++ : n_chunks;
     };
 
     uint32_t cand = 0;
@@ -225,6 +299,7 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
     const int n_fams = p.fam_end - p.fam_begin;
     for (int fi = 0; fi < n_fams; ++fi) {
         const int f = p.fam_begin + fi;
+        const FamilyDesc F = p.fams[f];
         if (fi > 0) __syncthreads();  // every warp is done with the previous tables
         {
             const uint4 *src = reinterpret_cast<const uint4 *>(fa.tables + (size_t)fi * fa.tab_bytes);
@@ -233,32 +308,59 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
             for (int i = t; i < (int)(sizeof(SeedFam) / 16); i += kFilterThreads)
                 reinterpret_cast<uint4 *>(sSF)[i] =
                     __ldg(reinterpret_cast<const uint4 *>(fa.fams + fi) + i);
+            if (ISM) {
+                const uint2 sz = fa.fam_sizes[fi];
+                // the family's descriptors (16 bits: the host checked that
+                // every entry start fits 12 bits and every count 4), the
+                // entries' guide indices and the family's guide planes
+                const SeedFam &gf = fa.fams[fi];
+                const uint32_t off0 = gf.seg[0].off, list0 = gf.list_off;
+                uint16_t *dOff = reinterpret_cast<uint16_t *>(sIdxBlk);
+                uint16_t *dIdx = dOff + sz.x;
+                uint2 *dG =
+                    reinterpret_cast<uint2 *>(sIdxBlk + ((sz.x * 2u + sz.y * 2u + 15u) & ~15u));
+                for (uint32_t i = t; i < sz.x; i += kFilterThreads) {
+                    const uint32_t d = __ldg(fa.offsets + off0 + i);
+                    dOff[i] = (uint16_t)((d & 0xFFFu) | ((d >> 16) << 12));
+                }
+                for (uint32_t i = t; i < sz.y; i += kFilterThreads)
+                    dIdx[i] = __ldg(fa.entry_idx + list0 + i);
+                for (int i = t; i < F.gend - F.gbeg; i += kFilterThreads) {
+                    const GuideRec g = p.guides[F.gbeg + i];
+                    dG[i] = make_uint2(g.h & 0xFFFFFu, g.l & 0xFFFFFu);
+                }
+            }
         }
         __syncthreads();
         if (dead) continue;
 
-        const FamilyDesc F = p.fams[f];
         const uint32_t win_off = F.three_prime ? 0u : (uint32_t)F.plen;
-        const uint32_t gbeg = (uint32_t)F.gbeg;
         const int n_tests = sSF->n_tests;
-        uint32_t seg_off[S], seg_ent[S];
+        const bool all_fixed = sSF->pam_generic == 0;
+        FiltView<K> fv;
+        fv.gbeg = (uint32_t)F.gbeg;
+        if (ISM) {
+            const uint2 sz = fa.fam_sizes[fi];
+            fv.off16 = reinterpret_cast<const uint16_t *>(sIdxBlk);
+            fv.idx16 = fv.off16 + sz.x;
+            fv.gpl = reinterpret_cast<const uint2 *>(sIdxBlk + ((sz.x * 2u + sz.y * 2u + 15u) & ~15u));
+        } else {
+            fv.off16 = fv.idx16 = nullptr;
+            fv.gpl = nullptr;
+        }
 #pragma unroll
         for (int j = 0; j < S; ++j) {
-            seg_off[j] = sSF->seg[j].off;
-            seg_ent[j] = sSF->list_off + sSF->seg[j].ent;
+            fv.seg_off[j] = ISM ? sSF->seg[j].off - sSF->seg[0].off : sSF->seg[j].off;
+            fv.seg_ent[j] = (ISM ? 0u : sSF->list_off) + sSF->seg[j].ent;
         }
         int qn = 0;  // survivors queued (warp-uniform)
 
-        int64_t cur = claim(fi);
-        int64_t cend = cur + kClaimChunks < n_chunks ? cur + kClaimChunks : n_chunks;
+        round = run = run_end = 0;
+        int cur = next_chunk(fi);
         int buf = 0;
         if (cur < n_chunks) issue(cur, buf);
         while (cur < n_chunks) {
-            int64_t nxt = cur + 1;
-            if (nxt >= cend) {
-                nxt = claim(fi);
-                cend = nxt + kClaimChunks < n_chunks ? nxt + kClaimChunks : n_chunks;
-            }
+            const int nxt = next_chunk(fi);
             const bool has_next = nxt < n_chunks;
             if (has_next) issue(nxt, buf ^ 1);
             const bool ok = mbar_wait_bounded(bar0 + 8u * (uint32_t)buf, (phase >> buf) & 1u);
@@ -276,8 +378,9 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
             const uint32_t *wL = wH + C::kWords;
             const uint32_t *wN = wL + C::kWords;
             const bool second = cur >= chunks0;
-            const int64_t lc = second ? cur - chunks0 : cur;
-            const int64_t total_bp = second ? p.strand[1].total_bp : p.strand[0].total_bp;
+            const uint32_t lc = (uint32_t)(second ? cur - chunks0 : cur);
+            const uint32_t total_bp =
+                (uint32_t)(second ? p.strand[1].total_bp : p.strand[0].total_bp);
             int has_n = second ? p.strand[1].has_n : p.strand[0].has_n;
             if (has_n) {
                 uint32_t nw = 0;
@@ -285,62 +388,94 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                 has_n = __any_sync(0xFFFFFFFFu, nw != 0u);
             }
             const uint32_t strand_bit = second ? 0x80000000u : 0u;
-            const int64_t base = lc * CH;
-            const int64_t lim64 = total_bp - kSiteSpan - base;
-            const int lim = lim64 > CH ? CH : (int)lim64;
+            // positions [0, lim) of this chunk are scanned (total_bp - 26
+            // overall); total_bp < 2^32, and a chunk starts below total_bp - 26
+            const uint32_t base32 = lc * (uint32_t)CH;
+            const uint32_t left = total_bp - (uint32_t)kSiteSpan - base32;
+            const int lim = left > (uint32_t)CH ? CH : (int)left;
 
-            // PAM tests of the lane's words (funnel shifts + LOP3)
-            uint32_t pass[C::kRows], hw[C::kRows][2], lw[C::kRows][2];
-#pragma unroll
-            for (int u = 0; u < C::kRows; ++u) {
-                const int wi = u * 32 + lane;
-                const int rem = lim - 32 * wi;
-                pass[u] = rem >= 32 ? 0xFFFFFFFFu : (rem <= 0 ? 0u : (1u << rem) - 1u);
-                hw[u][0] = wH[wi];
-                hw[u][1] = wH[wi + 1];
-                lw[u][0] = wL[wi];
-                lw[u][1] = wL[wi + 1];
-            }
-#pragma unroll 1
-            for (int k = 0; k < n_tests; ++k) {
-                const uint32_t sh = sSF->pam_shift[k];
-                const uint4 m = sSF->pam_mask[k];
-                const bool generic = (sSF->pam_generic >> k) & 1u;
+            // PAM tests of the lane's words (funnel shifts + LOP3).  The
+            // families in use (NGG, NG, NNGRRT, NNNRRT, NRN) test only fixed
+            // bits; the allowed-set form runs only for S, W and the three-base
+            // codes.  A chunk with more passing positions than the list holds
+            // runs the tests again for each further pass, so that no pass word
+            // stays live through the rounds.
+            auto pam_pass = [&](uint32_t (&pass)[C::kRows]) {
+                uint32_t hw[C::kRows][2], lw[C::kRows][2];
 #pragma unroll
                 for (int u = 0; u < C::kRows; ++u) {
-                    const uint32_t h = sfshr(hw[u][0], hw[u][1], sh);
-                    const uint32_t l = sfshr(lw[u][0], lw[u][1], sh);
-                    pass[u] &= generic ? (~h & ~l & m.x) | (~h & l & m.y) | (h & ~l & m.z) |
-                                             (h & l & m.w)
-                                       : ~(((h ^ m.x) & m.y) | ((l ^ m.z) & m.w));
+                    const int wi = u * 32 + lane;
+                    const int rem = lim - 32 * wi;
+                    pass[u] = rem >= 32 ? 0xFFFFFFFFu : (rem <= 0 ? 0u : (1u << rem) - 1u);
+                    hw[u][0] = wH[wi];
+                    hw[u][1] = wH[wi + 1];
+                    lw[u][0] = wL[wi];
+                    lw[u][1] = wL[wi + 1];
                 }
-            }
-            int cnt = 0;
+#pragma unroll 1
+                for (int k = 0; k < n_tests; ++k) {
+                    const uint32_t sh = sSF->pam_shift[k];
+                    const uint4 m = sSF->pam_mask[k];
+                    if (all_fixed || !((sSF->pam_generic >> k) & 1u)) {
 #pragma unroll
-            for (int u = 0; u < C::kRows; ++u) cnt += __popc(pass[u]);
-            int incl = cnt;
+                        for (int u = 0; u < C::kRows; ++u) {
+                            const uint32_t h = sfshr(hw[u][0], hw[u][1], sh);
+                            const uint32_t l = sfshr(lw[u][0], lw[u][1], sh);
+                            pass[u] &= ~(((h ^ m.x) & m.y) | ((l ^ m.z) & m.w));
+                        }
+                    } else {
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                if (lane >= o) incl += v;
-            }
-            const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            const int off0 = incl - cnt;
+                        for (int u = 0; u < C::kRows; ++u) {
+                            const uint32_t h = sfshr(hw[u][0], hw[u][1], sh);
+                            const uint32_t l = sfshr(lw[u][0], lw[u][1], sh);
+                            pass[u] &= (~h & ~l & m.x) | (~h & l & m.y) | (h & ~l & m.z) |
+                                       (h & l & m.w);
+                        }
+                    }
+                }
+            };
+            int total = 0, off0 = 0, cnt = 0;
 #pragma unroll 1
             for (int pass_i = 0; pass_i < C::kPasses; ++pass_i) {
+                uint32_t pass[C::kRows];
+                pam_pass(pass);
+                if (pass_i == 0) {
+#pragma unroll
+                    for (int u = 0; u < C::kRows; ++u) cnt += __popc(pass[u]);
+                    int incl = cnt;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                        if (lane >= o) incl += v;
+                    }
+                    total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+                    off0 = incl - cnt;
+                }
                 const int lo = pass_i * C::kListCap;
                 if (lo >= total) break;
                 const int n_list = min(total - lo, C::kListCap);
-                // list positions [lo, lo + n_list) of the chunk's passing positions
+                // list positions [lo, lo + n_list) of the chunk's passing
+                // positions (the order within a lane's word is irrelevant: each
+                // word is walked from its highest passing bit)
                 if (total <= C::kListCap) {
-                    int off = off0;
+                    uint16_t *out = wList + off0;
 #pragma unroll
                     for (int u = 0; u < C::kRows; ++u) {
                         uint32_t m = pass[u];
+                        const uint32_t wb = 32u * (uint32_t)(u * 32 + lane) + 31u;
+                        // two steps without a loop branch (most words hold at
+                        // most two passing positions), then the rest
+#pragma unroll
+                        for (int it = 0; it < 2; ++it) {
+                            const uint32_t z = __clz(m);
+                            if (m) *out = (uint16_t)(wb - z);
+                            out += m ? 1 : 0;
+                            m &= ~(uint32_t)(0x80000000ull >> z);  // z = 32 when m = 0
+                        }
                         while (m) {
-                            const int j = __ffs(m) - 1;
-                            m &= m - 1u;
-                            wList[off++] = (uint16_t)(32 * (u * 32 + lane) + j);
+                            const uint32_t z = __clz(m);
+                            m ^= 0x80000000u >> z;
+                            *out++ = (uint16_t)(wb - z);
                         }
                     }
                 } else if (off0 + cnt > lo && off0 < lo + n_list) {
@@ -348,30 +483,32 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
 #pragma unroll
                     for (int u = 0; u < C::kRows; ++u) {
                         uint32_t m = pass[u];
+                        const uint32_t wb = 32u * (uint32_t)(u * 32 + lane) + 31u;
                         while (m) {
-                            const int j = __ffs(m) - 1;
-                            m &= m - 1u;
-                            if ((unsigned)off < (unsigned)n_list)
-                                wList[off] = (uint16_t)(32 * (u * 32 + lane) + j);
+                            const uint32_t z = __clz(m);
+                            m ^= 0x80000000u >> z;
+                            if ((unsigned)off < (unsigned)n_list) wList[off] = (uint16_t)(wb - z);
                             ++off;
                         }
                     }
                 }
                 __syncwarp();
-                for (int k0 = 0; k0 < n_list; k0 += 32) {
-                    const int k = k0 + lane;
-                    const bool has = k < n_list;
-                    uint32_t s = 0, h20 = 0, l20 = 0;
-                    bool keep = false;
-                    if (has) {
-                        s = wList[k];
+                for (int k0 = 0; k0 < n_list; k0 += 32 * kFilterPer) {
+                    // filter: one byte per region key (bit 0: a guide's key
+                    // equals it; bits 1-7: colours of the guides within one
+                    // mismatch of it).  Lanes past the list read entry 0 and
+                    // keep nothing.
+                    uint32_t sv[kFilterPer], hv[kFilterPer], lv[kFilterPer];
+                    bool keep[kFilterPer];
+#pragma unroll
+                    for (int v = 0; v < kFilterPer; ++v) {
+                        const int k = k0 + v * 32 + lane;
+                        const bool has = k < n_list;
+                        const uint32_t s = wList[has ? k : 0];
                         const uint32_t wo = s + win_off;
                         const uint32_t wi = wo >> 5, b = wo & 31u;
-                        h20 = sfshr(wH[wi], wH[wi + 1], b);
-                        l20 = sfshr(wL[wi], wL[wi + 1], b);
-                        // filter: one byte per region key (bit 0: a guide's key
-                        // equals it; bits 1-7: colours of the guides within one
-                        // mismatch of it)
+                        const uint32_t h20 = sfshr(wH[wi], wH[wi + 1], b);
+                        const uint32_t l20 = sfshr(wL[wi], wL[wi + 1], b);
                         uint32_t x[S];
 #pragma unroll
                         for (int j = 0; j < S; ++j) {
@@ -383,38 +520,44 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                         uint32_t any = 0;
 #pragma unroll
                         for (int j = 0; j < S; ++j) any |= x[j];
+                        bool kp;
                         if constexpr (FT::M <= 1) {
-                            keep = (any & 0xFEu) != 0u;
+                            kp = (any & 0xFEu) != 0u;
                         } else if constexpr (FT::M > S) {
-                            keep = (any & 1u) != 0u;
+                            kp = (any & 1u) != 0u;
                         } else {
-                            keep = ((any & 1u) | (at_least_two<S>(x) & 0xFEu)) != 0u;
+                            kp = ((any & 1u) | (at_least_two<S>(x) & 0xFEu)) != 0u;
                         }
+                        sv[v] = s;
+                        hv[v] = h20;
+                        lv[v] = l20;
+                        keep[v] = has && kp;
                     }
-                    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
-                    if (bal) {
-                        if (keep) {
+#pragma unroll
+                    for (int v = 0; v < kFilterPer; ++v) {
+                        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep[v]);
+                        if (bal) {
+                            const uint32_t s = sv[v];
                             uint32_t n20g = 0;
                             if (has_n) {
+                                const uint32_t wo = s + win_off;
                                 const uint32_t n26 =
                                     sfshr(wN[s >> 5], wN[(s >> 5) + 1], s & 31u) & 0x3FFFFFFu;
-                                if (n26) {
-                                    const uint32_t wo = s + win_off;
-                                    n20g = sfshr(wN[wo >> 5], wN[(wo >> 5) + 1], wo & 31u) &
-                                           0xFFFFFu;
-                                }
+                                const uint32_t n20 =
+                                    sfshr(wN[wo >> 5], wN[(wo >> 5) + 1], wo & 31u) & 0xFFFFFu;
+                                n20g = n26 ? n20 : 0u;
                             }
-                            const int at = qn + __popc(bal & ((1u << lane) - 1u));
-                            wQ[at] = make_uint4((h20 & 0xFFFFFu) | strand_bit, l20 & 0xFFFFFu, n20g,
-                                                (uint32_t)(base + s));
-                        }
-                        qn += __popc(bal);
-                        if (qn >= 32) {
-                            __syncwarp();
-                            filter_heavy<K>(p, fa, wQ[qn - 32 + lane], true, seg_off, seg_ent,
-                                            gbeg, cand);
-                            qn -= 32;
-                            __syncwarp();
+                            // a lane without a survivor stores into the spare slot
+                            const int at = keep[v] ? qn + __popc(bal & lt_mask) : kSurvCap;
+                            wQ[at] = make_uint4((hv[v] & 0xFFFFFu) | strand_bit, lv[v] & 0xFFFFFu,
+                                                n20g, base32 + s);
+                            qn += __popc(bal);
+                            if (qn >= 32) {
+                                __syncwarp();
+                                cand += filter_heavy<K, ISM>(p, fa, fv, wQ[qn - 32 + lane], true);
+                                qn -= 32;
+                                __syncwarp();
+                            }
                         }
                     }
                 }
@@ -428,7 +571,7 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
         if (qn > 0) {
             __syncwarp();
             const bool v = lane < qn;
-            filter_heavy<K>(p, fa, wQ[v ? lane : 0], v, seg_off, seg_ent, gbeg, cand);
+            cand += filter_heavy<K, ISM>(p, fa, fv, wQ[v ? lane : 0], v);
             __syncwarp();
         }
     }
@@ -438,35 +581,36 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
     if (t == 0 && sCand) atomicAdd(p.counter + 1, sCand);
 }
 
-template <int K, int CH>
+template <int K, int CH, int ISM>
 static int launch_filter_k(const ScanParams &p, const FilterArgs &fa, int sm_count,
                            cudaStream_t s) {
-    constexpr size_t smem = filter_smem_bytes<K, CH>();
-    static_assert(smem <= 227 * 1024, "filter form fits in shared memory");
-    static bool configured = false;
-    if (!configured) {
-        BGO_CUDA(cudaFuncSetAttribute(scan_filter_kernel<K, CH>,
+    const size_t smem = filter_smem_fixed<K, CH>() + (ISM ? (size_t)fa.idx_smem_bytes : 0);
+    static_assert(filter_smem_fixed<K, CH>() <= kFilterSmemLimit, "filter form fits in shared memory");
+    static size_t configured = 0;
+    if (smem > configured) {
+        BGO_CUDA(cudaFuncSetAttribute(scan_filter_kernel<K, CH, ISM>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
+        configured = smem;
     }
-    // one persistent CTA per SM; warps claim chunks from per-family counters
-    scan_filter_kernel<K, CH><<<(unsigned)sm_count, kFilterThreads, smem, s>>>(p, fa);
+    // one persistent CTA per SM; warps take chunks in a grid stride, then
+    // claim the rest from per-family counters
+    scan_filter_kernel<K, CH, ISM><<<(unsigned)sm_count, kFilterThreads, smem, s>>>(p, fa);
     BGO_CUDA(cudaGetLastError());
     return BGO_OK;
 }
 
-template <int CH>
+template <int CH, int ISM>
 static int launch_filter_ch(const ScanParams &p, const FilterArgs &fa, int sm_count,
                             cudaStream_t s) {
     switch (p.max_mm) {
-        case 0: return launch_filter_k<0, CH>(p, fa, sm_count, s);
-        case 1: return launch_filter_k<1, CH>(p, fa, sm_count, s);
-        case 2: return launch_filter_k<2, CH>(p, fa, sm_count, s);
-        case 3: return launch_filter_k<3, CH>(p, fa, sm_count, s);
-        case 4: return launch_filter_k<4, CH>(p, fa, sm_count, s);
-        case 5: return launch_filter_k<5, CH>(p, fa, sm_count, s);
-        case 6: return launch_filter_k<6, CH>(p, fa, sm_count, s);
-        case 7: return launch_filter_k<7, CH>(p, fa, sm_count, s);
+        case 0: return launch_filter_k<0, CH, ISM>(p, fa, sm_count, s);
+        case 1: return launch_filter_k<1, CH, ISM>(p, fa, sm_count, s);
+        case 2: return launch_filter_k<2, CH, ISM>(p, fa, sm_count, s);
+        case 3: return launch_filter_k<3, CH, ISM>(p, fa, sm_count, s);
+        case 4: return launch_filter_k<4, CH, ISM>(p, fa, sm_count, s);
+        case 5: return launch_filter_k<5, CH, ISM>(p, fa, sm_count, s);
+        case 6: return launch_filter_k<6, CH, ISM>(p, fa, sm_count, s);
+        case 7: return launch_filter_k<7, CH, ISM>(p, fa, sm_count, s);
         default:
             set_error("prefiltered segment index: max_mismatches outside 0..7");
             return BGO_ERR_ARG;

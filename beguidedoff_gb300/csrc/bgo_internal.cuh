@@ -125,8 +125,14 @@ struct FilterArgs {
     const uint8_t *tables;     // per launch family, tab_bytes each
     uint32_t *work;            // per launch family: next chunk to claim
     int *err;                  // bit 0: a chunk copy wait gave up
+    const uint2 *fam_sizes;    // per launch family: (descriptors, list entries)
     int32_t tab_bytes;
     int32_t n_fams;
+    // bytes of the largest launch family's index in shared memory (16-bit
+    // descriptors, entry guide indices, guide planes); 0 = the index is read
+    // from global memory
+    int32_t idx_smem_bytes;
+    int32_t pad;
 };
 
 // Segment-mask scan (scan mode 3): the segment index stored as guide bitmasks.
@@ -249,6 +255,10 @@ struct bgo_plan {
     bgo::SeedArgs seed;
     std::vector<bgo::SeedArgs> seed_fam;  // the same index, one family per launch
     unsigned char *d_seed_fam;            // rebased per-family SeedFam copies
+    std::vector<uint2> seed_sizes;        // per family: (descriptors, list entries)
+    std::vector<uint32_t> seed_maxcnt;    // per family: largest bucket
+    std::vector<uint32_t> seed_maxreg;    // per family: longest region list
+    uint2 *d_seed_sizes = nullptr;
     // segment-mask index for one (max_mismatches, group size) pair
     int mask_k;               // -1000 = not built
     int mask_group;           // guides per group it was built with
@@ -289,6 +299,8 @@ size_t mask_smem_bytes(const MaskArgs &ma);
 bool build_filter_tables(const FamilyDesc *fams, int n_fams, const GuideRec *recs, int K,
                          std::vector<uint8_t> &tables, uint32_t &tab_bytes);
 uint32_t filter_tab_bytes(int K);
+// dynamic shared memory of a prefiltered form besides the survivor index
+size_t filter_smem_fixed_bytes(int K, int chunk_sites);
 int launch_filter_kernel(const ScanParams &p, const FilterArgs &fa, int sm_count, int chunk_sites,
                          cudaStream_t s);
 int launch_mask_kernel(const ScanParams &p, const MaskArgs &ma, int sm_count, int ctas_per_sm,

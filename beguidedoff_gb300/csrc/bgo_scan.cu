@@ -400,6 +400,7 @@ extern "C" int bgo_plan_destroy(bgo_plan *pl) {
     pool_free(pl->device, pl->d_guides);
     pool_free(pl->device, pl->d_seed);
     pool_free(pl->device, pl->d_seed_fam);
+    pool_free(pl->device, pl->d_seed_sizes);
     pool_free(pl->device, pl->d_mask);
     pool_free(pl->device, pl->d_filter);
     event_give(pl->device, pl->done);
@@ -543,8 +544,10 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
         BGO_CUDA(cudaEventSynchronize(pl->done));  // launches that read the old index
         BGO_CUDA(pool_free(pl->device, pl->d_seed));
         BGO_CUDA(pool_free(pl->device, pl->d_seed_fam));
+        BGO_CUDA(pool_free(pl->device, pl->d_seed_sizes));
         pl->d_seed = nullptr;
         pl->d_seed_fam = nullptr;
+        pl->d_seed_sizes = nullptr;
         pl->index_gen++;
     }
     pl->seed_fam.clear();
@@ -586,10 +589,22 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
     // own lists and bucket tables
     std::vector<SeedFam> rebased(sf);
     std::vector<SeedArgs> views(sf.size());
+    pl->seed_sizes.assign(sf.size(), make_uint2(0, 0));
+    pl->seed_maxcnt.assign(sf.size(), 0);
+    pl->seed_maxreg.assign(sf.size(), 0);
     for (size_t f = 0; f < sf.size(); ++f) {
         const uint32_t off0 = sf[f].seg[0].off;
         const uint32_t off_end = f + 1 < sf.size() ? sf[f + 1].seg[0].off : (uint32_t)offs.size();
         const uint32_t list_end = f + 1 < sf.size() ? sf[f + 1].list_off : (uint32_t)ents.size();
+        pl->seed_sizes[f] = make_uint2(off_end - off0, list_end - sf[f].list_off);
+        for (uint32_t i = off0; i < off_end; ++i)
+            pl->seed_maxcnt[f] = std::max(pl->seed_maxcnt[f], offs[i] >> 16);
+        // the longest region list of the family (descriptor starts index into it)
+        for (int j = 0; j < sf[f].nseg; ++j) {
+            const uint32_t end = j + 1 < sf[f].nseg ? sf[f].seg[j + 1].ent
+                                                    : list_end - sf[f].list_off;
+            pl->seed_maxreg[f] = std::max(pl->seed_maxreg[f], end - sf[f].seg[j].ent);
+        }
         rebased[f].list_off = 0;
         for (int j = 0; j < sf[f].nseg; ++j) rebased[f].seg[j].off = sf[f].seg[j].off - off0;
         SeedArgs v{};
@@ -606,8 +621,12 @@ static int seed_prepare(bgo_engine *engine, bgo_plan *pl, int K, cudaStream_t s)
                         sizeof(SeedFam) * (rebased.size() + 1)));
     BGO_CUDA(cudaMemcpyAsync(pl->d_seed_fam, rebased.data(), sizeof(SeedFam) * rebased.size(),
                              cudaMemcpyHostToDevice, s));
+    BGO_CUDA(pool_alloc(pl->device, (void **)&pl->d_seed_sizes,
+                        sizeof(uint2) * (pl->seed_sizes.size() + 1)));
+    BGO_CUDA(cudaMemcpyAsync(pl->d_seed_sizes, pl->seed_sizes.data(),
+                             sizeof(uint2) * pl->seed_sizes.size(), cudaMemcpyHostToDevice, s));
     BGO_CUDA(cudaStreamSynchronize(s));
-    engine->h2d_bytes += (int64_t)(sizeof(SeedFam) * rebased.size());
+    engine->h2d_bytes += (int64_t)((sizeof(SeedFam) + sizeof(uint2)) * rebased.size());
     for (size_t f = 0; f < views.size(); ++f)
         views[f].fams = reinterpret_cast<const SeedFam *>(pl->d_seed_fam) + f;
     pl->seed_fam = views;
@@ -799,6 +818,10 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
                 q.n_strands = n_strands;
                 q.tiles_total = q.strand[0].n_tiles + (n_strands > 1 ? q.strand[1].n_tiles : 0);
                 if (q.tiles_total == 0) return BGO_OK;
+                if (q.tiles_total >= (1ll << 31)) {
+                    set_error("prefiltered segment index: more than 2^31 chunks");
+                    return BGO_ERR_ARG;
+                }
                 q.fam_begin = g0;
                 q.fam_end = g1;
                 FilterArgs fa{};
@@ -809,8 +832,27 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
                 fa.tables = plan->d_filter + (size_t)g0 * plan->filter_tab;
                 fa.work = engine->d_work;
                 fa.err = reinterpret_cast<int *>(engine->d_counter + 2);
+                fa.fam_sizes = plan->d_seed_sizes + g0;
                 fa.tab_bytes = (int32_t)plan->filter_tab;
                 fa.n_fams = g1 - g0;
+                // the survivor index goes to shared memory when the largest
+                // family's index fits beside the tables and slices and its
+                // descriptors fit 16 bits (entry starts < 4096, counts < 16)
+                size_t need = 0;
+                bool fits16 = true;
+                for (int g = g0; g < g1; ++g) {
+                    const uint2 sz = plan->seed_sizes[(size_t)g];
+                    const size_t G = (size_t)(plan->h_fams[g].gend - plan->h_fams[g].gbeg);
+                    fits16 = fits16 && plan->seed_maxreg[(size_t)g] <= 4096 &&
+                             plan->seed_maxcnt[(size_t)g] <= 15;
+                    need = std::max(need, ((size_t)sz.x * 2 + (size_t)sz.y * 2 + 15) / 16 * 16 +
+                                              (G * 8 + 15) / 16 * 16);
+                }
+                fa.idx_smem_bytes =
+                    fits16 && filter_smem_fixed_bytes(max_mismatches, chunk) + need <=
+                                  (size_t)(227 * 1024)
+                        ? (int32_t)need
+                        : 0;
                 BGO_CUDA(cudaMemsetAsync(engine->d_work, 0, sizeof(uint32_t) * (size_t)(g1 - g0), s));
                 rc = launch_filter_kernel(q, fa, engine->sm_count, chunk, s);
                 if (rc != BGO_OK) return rc;
