@@ -16,14 +16,30 @@ minimal stand-ins into ``sys.modules`` *before* the reference is imported:
   finder's device check passes; tensors are never used by the kernel.
 
 This file is used only by ``make_golden.py`` to record reference outputs; it is
-never imported by the product or by the tests that run on the GPU machine.
+never imported by the product or by the tests that run on the GPU machine.  The
+reference checkout is found through the ``BGO_REFERENCE_ROOT`` environment
+variable (``make_golden.py --reference DIR`` sets it).
+
+``set_workers(n)`` makes a kernel launch run its blocks in ``n`` forked worker
+processes, each over a contiguous block range with its own zeroed hit
+counters; the parent appends the workers' hits in block order after the hits
+already recorded, which is exactly the sequential run's atomic order (genome
+order), with the same per-guide cap and exact counts.
 """
+import multiprocessing
+import os
 import sys
 import types
 
 import numpy as np
 
-REFERENCE_ROOT = "/root/reference"
+REFERENCE_ROOT = os.environ.get("BGO_REFERENCE_ROOT", "")
+_WORKERS = 1
+
+
+def set_workers(n):
+    global _WORKERS
+    _WORKERS = max(1, int(n))
 
 
 # ----------------------------------------------------------------------------
@@ -45,14 +61,40 @@ class _Kernel:
     def __getitem__(self, cfg):
         grid, block = cfg
 
-        def launch(*args):
+        def run(args, lo, hi):
             cuda = _cuda
             cuda.blockDim.x = 1
             cuda.threadIdx.x = 0
-            total = int(grid) * int(block)
-            for b in range(total):
+            for b in range(lo, hi):
                 cuda.blockIdx.x = b
                 self.fn(*args)
+
+        def launch(*args):
+            total = int(grid) * int(block)
+            if _WORKERS == 1 or total < 4 * _WORKERS:
+                run(args, 0, total)
+                return
+            # the search kernel's last three arguments are its outputs: per-guide
+            # counters, positions and mismatches (beguidedoff/cuda_search.py:177-180)
+            counts, hpos, hmm = args[-3], args[-2], args[-1]
+            rpg = hpos.shape[1]
+            bounds = np.linspace(0, total, _WORKERS + 1).astype(np.int64)
+            # the workers are forked after this, so they inherit the kernel and
+            # its arguments without pickling them
+            _ACTIVE["fn"], _ACTIVE["args"] = self.fn, args
+            ctx = multiprocessing.get_context("fork")
+            with ctx.Pool(_WORKERS) as pool:
+                parts = pool.starmap(_worker_run, [(int(bounds[w]), int(bounds[w + 1]))
+                                                   for w in range(_WORKERS)])
+            _ACTIVE.clear()
+            for lc, lp, lm in parts:
+                for g in range(counts.shape[0]):
+                    k, c0 = int(lc[g]), int(counts[g])
+                    keep = max(0, min(k, rpg - c0))
+                    if keep:
+                        hpos[g, c0:c0 + keep] = lp[g, :keep]
+                        hmm[g, c0:c0 + keep] = lm[g, :keep]
+                    counts[g] = c0 + k
 
         return launch
 
@@ -77,6 +119,26 @@ class _Atomic:
         old = int(arr[idx])
         arr[idx] = old + int(val)
         return old
+
+
+_ACTIVE = {}
+
+
+def _worker_run(lo, hi):
+    """Blocks [lo, hi) of the active launch with fresh outputs; returns
+    (counts, positions, mismatches)."""
+    fn, args = _ACTIVE["fn"], _ACTIVE["args"]
+    counts, hpos, hmm = args[-3], args[-2], args[-1]
+    lc = np.zeros_like(counts)
+    lp = np.zeros_like(hpos)
+    lm = np.zeros_like(hmm)
+    local = tuple(args[:-3]) + (lc, lp, lm)
+    _cuda.blockDim.x = 1
+    _cuda.threadIdx.x = 0
+    for b in range(lo, hi):
+        _cuda.blockIdx.x = b
+        fn(*local)
+    return lc, lp, lm
 
 
 _cuda = types.SimpleNamespace(
@@ -213,6 +275,9 @@ def install():
     Returns the tuple (beguidedoff package, finder module, cuda_search module,
     genome_converter module).
     """
+    if not REFERENCE_ROOT or not os.path.isdir(os.path.join(REFERENCE_ROOT, "beguidedoff")):
+        raise SystemExit("set BGO_REFERENCE_ROOT (or make_golden.py --reference) to the "
+                         "reference checkout")
     sys.dont_write_bytecode = True
     sys.modules.setdefault("numba", _make_numba())
     sys.modules.setdefault("pandas", _make_pandas())

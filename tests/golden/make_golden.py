@@ -2,7 +2,7 @@
 
 Usage (in a container that has the reference checkout; the GPU machine does not):
 
-    python tests/golden/make_golden.py [--only NAME ...]
+    python tests/golden/make_golden.py --reference DIR [--only NAME ...] [--workers N]
 
 Each case writes ``tests/golden/<name>.npz`` holding
 
@@ -31,6 +31,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
+if "--reference" in sys.argv:
+    os.environ["BGO_REFERENCE_ROOT"] = sys.argv[sys.argv.index("--reference") + 1]
 import _refshim  # noqa: E402
 
 REF, F, CS, GC = _refshim.install()
@@ -515,6 +517,56 @@ def case_convert():
     print("convert: ok")
 
 
+def case_config1():
+    """The plain CPU-runnable configuration at its stated size (10 Mbp, 2
+    chromosomes, 1% N in runs of 100-5,000 bp, 10 NGG guides x 20 planted
+    sites with 0-4 substitutions, ABE window 4-8, max_mismatches 4), generated
+    by config1.py.  The fixture keeps the hashes of the genome arrays the
+    reference's converter wrote, not the arrays."""
+    import config1 as C1
+
+    t0 = time.time()
+    chroms, guides_seq, on = C1.generate()
+    guides = C1.guide_inputs(GuideInput, guides_seq, on)
+    runs = [{"kwargs": {"return_all": True, "count_score_threshold": 5.0}},
+            {"kwargs": {"return_all": False, "count_score_threshold": 40.0}}]
+    with tempfile.TemporaryDirectory() as td:
+        fa = os.path.join(td, "genome.fa")
+        npz = os.path.join(td, "genome.npz")
+        with open(fa, "w") as fh:
+            for name, seq in chroms:
+                fh.write(f">{name}\n")
+                text = seq.decode()
+                for i in range(0, len(text), 60):
+                    fh.write(text[i:i + 60] + "\n")
+        GC.convert(fa, npz, include_n_mask=True, verbose=False)
+        gd = GC.load_genome(npz)
+        fixture = {
+            "chrom_names": np.array([str(c) for c in gd["chrom_names"]]),
+            "chrom_offsets": gd["chrom_offsets"],
+            "chrom_lengths": gd["chrom_lengths"],
+            "total_bp": np.int64(gd["total_bp"]),
+            "sha_forward": np.array(C1.digest(gd["genome_forward"])),
+            "sha_rc": np.array(C1.digest(gd["genome_rc"])),
+            "sha_n_mask": np.array(C1.digest(gd["n_mask"])),
+        }
+        fixture.update(guide_arrays(guides))
+        finder = REF.beguidedoff(genome_path=npz, max_mismatches=C1.MAX_MISMATCHES,
+                                 n_top_offtargets=3, device="cuda:0")
+        meta = {"name": "config1", "max_mismatches": C1.MAX_MISMATCHES, "n_top_offtargets": 3,
+                "results_per_guide": 10240, "max_results_per_guide": None, "runs": [],
+                "raw_calls": 0}
+        for ri, run in enumerate(runs):
+            with _refshim_capture_warnings() as warns:
+                df = finder.search(guides=guides, verbose=False, **run["kwargs"])
+            fixture.update(table_arrays(df, f"r{ri}_"))
+            meta["runs"].append({"kwargs": run["kwargs"], "n_rows": len(df),
+                                 "warnings": warns.messages, "raw_calls": []})
+        fixture["meta_json"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, "config1.npz"), **fixture)
+    print(f"config1: {[r['n_rows'] for r in meta['runs']]} rows, {time.time() - t0:.1f}s")
+
+
 CASES = {
     "planted_ngg": case_planted_ngg,
     "mixed_pam": case_mixed_pam,
@@ -524,12 +576,17 @@ CASES = {
     "many_guides": case_many_guides,
     "seam_5prime": case_seam_5prime,
     "convert": case_convert,
+    "config1": case_config1,
 }
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", nargs="*")
+    ap.add_argument("--reference", help="reference checkout (sets BGO_REFERENCE_ROOT)")
+    ap.add_argument("--workers", type=int, default=1,
+                    help="processes the shim runs each kernel launch in")
     a = ap.parse_args()
+    _refshim.set_workers(a.workers)
     for name, fn in CASES.items():
         if a.only and name not in a.only:
             continue
