@@ -24,13 +24,16 @@ EXPORTED = [
     "bgo_genome_create", "bgo_genome_destroy", "bgo_genome_info", "bgo_engine_create",
     "bgo_engine_destroy", "bgo_plan_create", "bgo_plan_destroy", "bgo_plan_info",
     "bgo_scan_launch", "bgo_scan_collect", "bgo_engine_reserve", "bgo_search_genome",
-    "bgo_engine_info", "bgo_synth_genome", "bgo_probe_int_throughput", "bgo_scan_stats",
+    "bgo_engine_info", "bgo_scan_stats",
     "bgo_scan_noalloc", "bgo_graph_create", "bgo_graph_launch", "bgo_graph_destroy",
-    "bgo_epilogue_run", "bgo_synth_genome_repeats", "bgo_engine_transfer",
+    "bgo_epilogue_run", "bgo_engine_transfer",
     "bgo_plan_set_tuning", "bgo_epilogue_fetch", "bgo_scan_time", "bgo_stream_create",
     "bgo_stream_destroy", "bgo_plan_families", "bgo_plan_set_family_tuning",
-    "bgo_genome_upload", "bgo_encode_genome",
+    "bgo_genome_upload", "bgo_encode_genome", "bgo_scan_complete",
 ]
+
+# Names of every function declared in include/bgo_tools.h (libbgo_tools.so).
+TOOLS_EXPORTED = ["bgo_synth_genome", "bgo_synth_genome_repeats", "bgo_probe_int_throughput"]
 
 INPUT_ROW_DTYPE = np.dtype([("plan_row", "<i4"), ("window_mask", "<u4"), ("target_base", "<i4"),
                             ("ot_chrom", "<i4"), ("ot_local", "<i8"), ("ot_strand", "<i4"),
@@ -101,6 +104,7 @@ _SIGS = {
     "bgo_engine_info": ([_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)], ctypes.c_int),
     "bgo_engine_transfer": ([_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64)], ctypes.c_int),
     "bgo_plan_set_tuning": ([_P, _P], ctypes.c_int),
+    "bgo_scan_complete": ([_P, _P, _P, _P, _I32, _I32, _I32, _P, _P], ctypes.c_int),
     "bgo_synth_genome": ([ctypes.c_uint64, _P, _I32, _P, _P, _I64, _P, ctypes.c_int, _P, _P, _P],
                          ctypes.c_int),
     "bgo_probe_int_throughput": ([ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
@@ -142,7 +146,7 @@ def synth_genome(seed, chrom_lengths, n_blocks=(), thresholds=(64, 128, 192), de
         assert fwd.size >= n_words and rc.size >= n_words and nm.size >= n_bytes
     fams = None
     if repeats is None:
-        check(lib().bgo_synth_genome(int(seed), ptr(lens), lens.size, ptr(starts), ptr(ends),
+        check(tools_lib().bgo_synth_genome(int(seed), ptr(lens), lens.size, ptr(starts), ptr(ends),
                                      starts.size, ptr(th), int(device), fwd.ctypes.data,
                                      rc.ctypes.data, nm.ctypes.data), "bgo_synth_genome")
     else:
@@ -151,7 +155,7 @@ def synth_genome(seed, chrom_lengths, n_blocks=(), thresholds=(64, 128, 192), de
                           int(round(float(repeats["divergence"]) * 65536)), 0,
                           int(repeats.get("seed", seed)))
         fams = np.zeros(spec.n_families * spec.family_len, dtype=np.uint8)
-        check(lib().bgo_synth_genome_repeats(
+        check(tools_lib().bgo_synth_genome_repeats(
             int(seed), ptr(lens), lens.size, ptr(starts), ptr(ends), starts.size, ptr(th),
             ctypes.byref(spec), fams.ctypes.data, int(device), fwd.ctypes.data, rc.ctypes.data,
             nm.ctypes.data), "bgo_synth_genome_repeats")
@@ -192,7 +196,7 @@ def encode_genome(seq: bytes, chrom_lengths, include_rc=True, include_n_mask=Tru
 def probe_int_throughput(op, device=0):
     """Measured Gop/s of LOP3 (op 0), POPC (1) or 32-bit add (2)."""
     v = ctypes.c_double()
-    check(lib().bgo_probe_int_throughput(int(device), int(op), ctypes.byref(v)),
+    check(tools_lib().bgo_probe_int_throughput(int(device), int(op), ctypes.byref(v)),
           "bgo_probe_int_throughput")
     return v.value
 
@@ -212,11 +216,34 @@ def lib():
                 "`python -c 'import beguidedoff_gb300.build as b; b.build()'` (needs nvcc)")
         L = ctypes.CDLL(path)
         for name, (args, res) in _SIGS.items():
+            if name in TOOLS_EXPORTED:
+                continue
             fn = getattr(L, name)
             fn.argtypes = args
             fn.restype = res
         _LIB = L
     return _LIB
+
+
+_TOOLS = None
+
+
+def tools_lib():
+    """The tools library (synthetic genomes, integer-pipe probe)."""
+    global _TOOLS
+    if _TOOLS is None:
+        lib()
+        path = _build.TOOLS_PATH
+        if not os.path.exists(path):
+            raise NativeLibraryMissing(f"tools library {path} is not built")
+        L = ctypes.CDLL(path)
+        for name in TOOLS_EXPORTED:
+            args, res = _SIGS[name]
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _TOOLS = L
+    return _TOOLS
 
 
 def last_error():
@@ -462,16 +489,25 @@ class Engine:
     def reserve(self, n_hits):
         check(lib().bgo_engine_reserve(self.handle, int(n_hits)), "bgo_engine_reserve")
 
+    def complete(self, plan, strands, n_encoded, max_mismatches, mode=1, stream=None):
+        """After launch(): makes the hit buffer hold every hit of that scan
+        (bgo_scan_complete: on overflow, grows it and rescans only the
+        granules whose keys were dropped); returns the exact hit count."""
+        arr = (ctypes.c_void_p * len(strands))(*[s.handle.value for s in strands])
+        ne = np.ascontiguousarray(n_encoded, dtype=np.int32)
+        n = ctypes.c_int64()
+        check(lib().bgo_scan_complete(self.handle, plan.handle, arr, ptr(ne), len(strands),
+                                      int(max_mismatches), int(mode), stream, ctypes.byref(n)),
+              "bgo_scan_complete")
+        return n.value
+
     def scan(self, plan, strands, n_encoded, max_mismatches, mode=1, stream=None):
-        """Launch + collect, growing the hit buffer and re-running on overflow."""
+        """Launch + complete + collect: every hit key, sorted."""
         self.launch(plan, strands, n_encoded, max_mismatches, mode, stream)
+        self.complete(plan, strands, n_encoded, max_mismatches, mode, stream)
         n, keys = self.collect(stream)
         if keys is None:
-            self.reserve(n)
-            self.launch(plan, strands, n_encoded, max_mismatches, mode, stream)
-            n, keys = self.collect(stream)
-            if keys is None:
-                raise BgoError(BGO_ERR_STATE, "scan", "hit buffer overflow after reserve")
+            raise BgoError(BGO_ERR_STATE, "scan", "hit buffer overflow after completion")
         return keys
 
     def info(self):

@@ -106,6 +106,22 @@ cudaError_t pool_free(int device, void *p) {
     return cudaFreeAsync(p, fs);
 }
 
+cudaError_t pool_free_after(int device, void *p, cudaStream_t stream) {
+    if (!p) return cudaSuccess;
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t fs = nullptr;
+    cudaError_t e = device_pool(device, &pool, &fs);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t ev = nullptr;
+    e = event_take(device, &ev);
+    if (e == cudaSuccess) e = cudaEventRecord(ev, stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(fs, ev, 0);
+    if (e == cudaSuccess) e = cudaFreeAsync(p, fs);
+    // the event may be re-recorded once the free stream has taken its wait
+    event_give(device, ev);
+    return e;
+}
+
 static thread_local std::string g_last_error;
 
 void set_error(const std::string &msg) { g_last_error = msg; }

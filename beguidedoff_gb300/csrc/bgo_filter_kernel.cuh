@@ -252,9 +252,11 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
     }
     __syncwarp();
 
-    // chunk indices fit 32 bits (the host checks tiles_total < 2^31)
+    // chunk indices fit 32 bits (the host checks tiles_total < 2^31); a
+    // rescan scans only the chunks of its list (items index the list)
     const int chunks0 = (int)p.strand[0].n_tiles;
-    const int n_chunks = (int)p.tiles_total;
+    const int n_chunks = p.chunk_list ? (int)p.n_list : (int)p.tiles_total;
+    auto chunk_at = [&](int i) -> int { return p.chunk_list ? (int)p.chunk_list[i] : i; };
     // Copies chunk c's words [c*CH/32, c*CH/32 + kWords) of the three planes
     // into buffer b (the planes are padded so that the copy never leaves them,
     // and zero beyond total_bp).  One lane issues the three bulk copies.
@@ -358,11 +360,11 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
         round = run = run_end = 0;
         int cur = next_chunk(fi);
         int buf = 0;
-        if (cur < n_chunks) issue(cur, buf);
+        if (cur < n_chunks) issue(chunk_at(cur), buf);
         while (cur < n_chunks) {
             const int nxt = next_chunk(fi);
             const bool has_next = nxt < n_chunks;
-            if (has_next) issue(nxt, buf ^ 1);
+            if (has_next) issue(chunk_at(nxt), buf ^ 1);
             const bool ok = mbar_wait_bounded(bar0 + 8u * (uint32_t)buf, (phase >> buf) & 1u);
             phase ^= 1u << buf;
             if (!__all_sync(0xFFFFFFFFu, ok)) {
@@ -377,8 +379,9 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
             const uint32_t *wH = reinterpret_cast<const uint32_t *>(slice + buf * C::kBuf);
             const uint32_t *wL = wH + C::kWords;
             const uint32_t *wN = wL + C::kWords;
-            const bool second = cur >= chunks0;
-            const uint32_t lc = (uint32_t)(second ? cur - chunks0 : cur);
+            const int chunk = chunk_at(cur);
+            const bool second = chunk >= chunks0;
+            const uint32_t lc = (uint32_t)(second ? chunk - chunks0 : chunk);
             const uint32_t total_bp =
                 (uint32_t)(second ? p.strand[1].total_bp : p.strand[0].total_bp);
             int has_n = second ? p.strand[1].has_n : p.strand[0].has_n;

@@ -54,6 +54,11 @@ struct StrandDesc {
     int32_t pad;
 };
 
+// Keys that do not fit the hit buffer mark their granule (kDropGranule
+// positions of one strand) in a bitmap, so that an overflowing scan rescans
+// only the granules whose keys were dropped.
+constexpr int64_t kDropGranule = 4096;
+
 struct ScanParams {
     StrandDesc strand[2];
     int32_t n_strands;
@@ -65,6 +70,14 @@ struct ScanParams {
     int64_t cap;
     unsigned long long *counter;
     int64_t tiles_total;
+    // granule bitmap of dropped keys (NULL: none); granules of strand slot 1
+    // start at drop_base1
+    uint32_t *drop_bits;
+    int64_t drop_base1;
+    // chunks to scan (NULL: all tiles_total); the chunk-indexed kernels
+    // (segment index, prefiltered) take this list on a rescan
+    const uint32_t *chunk_list;
+    int64_t n_list;
 };
 
 // Segment-indexed scan (scan mode 2): independent warps, each streaming chunks
@@ -189,6 +202,8 @@ int cuda_fail(cudaError_t e, const char *what);
 // memory that no queued work uses any more.
 cudaError_t pool_alloc(int device, void **p, size_t bytes);
 cudaError_t pool_free(int device, void *p);
+// frees p once the work queued on `stream` so far is done (no host wait)
+cudaError_t pool_free_after(int device, void *p, cudaStream_t stream);
 // a disable-timing event of the device's recycled set, and its return
 cudaError_t event_take(int device, cudaEvent_t *ev);
 void event_give(int device, cudaEvent_t ev);
@@ -332,6 +347,20 @@ struct bgo_engine {
     uint64_t keys_gen = 0;
     // per launch family: the prefiltered kernel's next chunk to claim
     uint32_t *d_work = nullptr;
+    // granule bitmap of keys dropped by the last scan (grow-only, from the pool)
+    uint32_t *d_drop = nullptr;
+    int64_t drop_words = 0;
+    // 1 while every launch of the last scan takes a chunk list (segment
+    // index, prefiltered), so that an overflow rescans dropped granules only
+    int last_listable = 0;
+    // a rescan in progress: the chunk lists per chunk length (1,024, 2,048,
+    // 4,096 positions) on the device, and their lengths
+    int rescan = 0;
+    const uint32_t *rescan_list[3] = {nullptr, nullptr, nullptr};
+    int64_t rescan_n[3] = {0, 0, 0};
+    // recorded after the last work that reads or writes d_keys; a resize
+    // waits on it (not on the device) before freeing the old buffer
+    cudaEvent_t keys_done = nullptr;
 };
 // counters of d_counter: hits, pairs evaluated, error flags (bit 0: a chunk
 // copy wait gave up), spare

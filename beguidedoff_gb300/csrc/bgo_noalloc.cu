@@ -8,7 +8,9 @@
 // cudaFree would synchronise the whole device in the middle of a request.  The
 // regular path (bgo_plan_create + bgo_scan_launch + bgo_scan_collect) allocates
 // the guide tables per plan and grows the engine's hit buffer on demand; this
-// entry point allocates nothing, on the device or on the host.
+// entry point allocates no device memory, and on success no host memory
+// either (its host-side family and guide tables are static arrays; a failing
+// call records its error message in a host string).
 //
 // Instead, all the scratch it needs lives in one file-scope static __device__
 // array (kNoallocBytes, about 8.1 MB): the hit counter and work counter, the
@@ -20,8 +22,10 @@
 // device is current, checks the result and caches it; make that first call
 // before any stream capture.  Every later call on the device reuses the same
 // array: each call clears the counters it relies on, and two calls whose work
-// overlaps on the GPU (different host threads, different streams) race on the
-// same memory, so callers must serialise them.
+// overlaps on the GPU (different streams) race on the same memory, so callers
+// must serialise them.  Host threads are serialised here: a call holds a mutex
+// from its checks to its last copy, since the static host tables are shared
+// too.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,10 +52,15 @@ static std::mutex g_noalloc_mutex;
 static unsigned char *g_noalloc_ptr[kMaxDevices];
 static int g_noalloc_blocks_per_sm[kMaxDevices];
 static int g_noalloc_sms[kMaxDevices];
+// host-side family and guide tables of a call (about 72 KB; static so that a
+// call needs no heap and no large stack frame), guarded by g_noalloc_mutex
+static FamilyDesc g_fams[kNoallocMaxGuides];
+static GuideRec g_recs[kNoallocMaxGuides];
+static int32_t g_fam_of[kNoallocMaxGuides];
 
-// Device address of the scratch array on `device` (current), looked up once.
+// Device address of the scratch array on `device` (current), looked up once;
+// the caller holds g_noalloc_mutex.
 static int noalloc_setup(int device, unsigned char **out) {
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (!g_noalloc_ptr[device]) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -92,27 +101,29 @@ extern "C" int bgo_scan_noalloc(const bgo_genome *const *strands, const int32_t 
                   " (BGO_NOALLOC_MAX_GUIDES); split the rows or use bgo_plan_create");
         return BGO_ERR_ARG;
     }
-    const int device = strands[0]->device;
     for (int i = 0; i < n_strands; ++i) {
-        if (!strands[i] || strands[i]->device != device || n_encoded[i] < 0 || n_encoded[i] > 3) {
+        if (!strands[i] || n_encoded[i] < 0 || n_encoded[i] > 3 ||
+            strands[i]->device != strands[0]->device) {
             set_error("bgo_scan_noalloc: bad strand or n_encoded");
             return BGO_ERR_ARG;
         }
     }
+    const int device = strands[0]->device;
     if (device < 0 || device >= kMaxDevices) {
         set_error("bgo_scan_noalloc: device index out of range");
         return BGO_ERR_ARG;
     }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     BGO_CUDA(cudaSetDevice(device));
     unsigned char *base = nullptr;
     int rc = noalloc_setup(device, &base);
     if (rc != BGO_OK) return rc;
     cudaStream_t s = (cudaStream_t)stream;
 
-    // PAM families and guide planes built in fixed-size host arrays (no heap).
-    FamilyDesc fams[kNoallocMaxGuides];
-    GuideRec recs[kNoallocMaxGuides];
-    int32_t fam_of[kNoallocMaxGuides];
+    // PAM families and guide planes built in the static host tables (no heap).
+    FamilyDesc *fams = g_fams;
+    GuideRec *recs = g_recs;
+    int32_t *fam_of = g_fam_of;
     int n_fams = 0;
     for (int32_t i = 0; i < n_guides; ++i) {
         fam_of[i] = -1;

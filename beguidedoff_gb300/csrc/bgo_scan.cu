@@ -30,6 +30,7 @@
 #include <string>
 #include <vector>
 
+#include "bgo_device.cuh"
 #include "bgo_internal.cuh"
 
 namespace bgo {
@@ -52,7 +53,8 @@ __device__ __forceinline__ uint32_t allowed_bits(uint32_t h, uint32_t l, uint32_
 
 // Appends `key`; the lanes executing this call together share one atomicAdd.
 __device__ __forceinline__ void emit_key(uint64_t key, uint64_t *keys, int64_t cap,
-                                         unsigned long long *counter) {
+                                         unsigned long long *counter, uint32_t *drop_bits,
+                                         int64_t drop_base1) {
     unsigned act = __activemask();
     int lane = threadIdx.x & 31;
     int leader = __ffs(act) - 1;
@@ -61,6 +63,7 @@ __device__ __forceinline__ void emit_key(uint64_t key, uint64_t *keys, int64_t c
     base = __shfl_sync(act, base, leader);
     unsigned long long slot = base + (unsigned long long)__popc(act & ((1u << lane) - 1u));
     if (slot < (unsigned long long)cap) keys[slot] = key;
+    else mark_dropped(key, drop_bits, drop_base1);
 }
 
 __global__ void __launch_bounds__(kTileThreads) scan_kernel(ScanParams p) {
@@ -186,7 +189,7 @@ __global__ void __launch_bounds__(kTileThreads) scan_kernel(ScanParams p) {
                                 const uint64_t pos = (uint64_t)(base + s);
                                 const uint64_t key = ((uint64_t)G.z << 39) | (slot << 38) |
                                                      (pos << 6) | (uint64_t)mmf;
-                                emit_key(key, p.keys, p.cap, p.counter);
+                                emit_key(key, p.keys, p.cap, p.counter, p.drop_bits, p.drop_base1);
                             }
                         }
                     }
@@ -229,11 +232,13 @@ extern "C" int bgo_engine_create(int device, bgo_engine **out) {
     if (ce == cudaSuccess)
         ce = cudaMemset(e->d_counter, 0, kEngineCounters * sizeof(unsigned long long));
     if (ce == cudaSuccess) ce = cudaMalloc(&e->d_work, kWorkCap * sizeof(uint32_t));
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->keys_done, cudaEventDisableTiming);
     int sms = 0;
     if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (ce != cudaSuccess) {
         if (e->d_counter) cudaFree(e->d_counter);
         if (e->d_work) cudaFree(e->d_work);
+        if (e->keys_done) cudaEventDestroy(e->keys_done);
         delete e;
         return cuda_fail(ce, "bgo_engine_create");
     }
@@ -245,9 +250,13 @@ extern "C" int bgo_engine_create(int device, bgo_engine **out) {
 extern "C" int bgo_engine_destroy(bgo_engine *e) {
     if (!e) return BGO_OK;
     cudaSetDevice(e->device);
-    if (e->d_keys) cudaFree(e->d_keys);
+    // the engine's queued work is done before its memory goes back
+    if (e->keys_done) cudaEventSynchronize(e->keys_done);
+    if (e->d_keys) pool_free(e->device, e->d_keys);
+    if (e->d_drop) pool_free(e->device, e->d_drop);
     if (e->d_counter) cudaFree(e->d_counter);
     if (e->d_work) cudaFree(e->d_work);
+    if (e->keys_done) cudaEventDestroy(e->keys_done);
     if (e->d_epi) cudaFree(e->d_epi);
     if (e->d_epi_rec) cudaFree(e->d_epi_rec);
     if (e->d_epi_out) cudaFree(e->d_epi_out);
@@ -262,10 +271,12 @@ extern "C" int bgo_engine_reserve(bgo_engine *e, int64_t n_hits) {
     BGO_CUDA(cudaSetDevice(e->device));
     int64_t cap = std::max<int64_t>(n_hits, e->cap * 2);
     uint64_t *p = nullptr;
-    BGO_CUDA(cudaMalloc(&p, (size_t)cap * sizeof(uint64_t)));
-    // the old buffer may still be written by work in flight on any stream
-    BGO_CUDA(cudaDeviceSynchronize());
-    if (e->d_keys) cudaFree(e->d_keys);
+    BGO_CUDA(pool_alloc(e->device, (void **)&p, (size_t)cap * sizeof(uint64_t)));
+    // the old buffer may still be read or written by the engine's last scan
+    // or epilogue: wait for that work only (not for the device, where other
+    // engines' scans may run), then return the buffer to the pool
+    BGO_CUDA(cudaEventSynchronize(e->keys_done));
+    if (e->d_keys) BGO_CUDA(pool_free(e->device, e->d_keys));
     e->d_keys = p;
     e->cap = cap;
     e->keys_gen++;
@@ -734,10 +745,41 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
     }
     BGO_CUDA(cudaSetDevice(engine->device));
     cudaStream_t s = (cudaStream_t)stream;
-    BGO_CUDA(cudaMemsetAsync(engine->d_counter, 0, kEngineCounters * sizeof(unsigned long long), s));
+    // granules of each strand (kDropGranule positions), for the bitmap of
+    // dropped keys
+    int64_t gran[2] = {0, 0};
+    for (int i = 0; i < n_strands; ++i)
+        gran[i] = std::max<int64_t>(0, ceil_div(strands[i]->total_bp - kSiteSpan, kDropGranule));
+    const int64_t drop_words = (gran[0] + gran[1]) / 32 + 1;
+    if (!engine->rescan) {
+        BGO_CUDA(cudaMemsetAsync(engine->d_counter, 0, kEngineCounters * sizeof(unsigned long long), s));
+        if (engine->drop_words < drop_words) {
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            BGO_CUDA(cudaStreamIsCapturing(s, &cs));
+            if (cs != cudaStreamCaptureStatusNone) {
+                set_error("bgo_scan_launch: the dropped-key bitmap must grow outside a capture");
+                return BGO_ERR_STATE;
+            }
+            if (engine->d_drop) {
+                BGO_CUDA(cudaEventSynchronize(engine->keys_done));
+                BGO_CUDA(pool_free(engine->device, engine->d_drop));
+                engine->d_drop = nullptr;
+            }
+            BGO_CUDA(pool_alloc(engine->device, (void **)&engine->d_drop,
+                                sizeof(uint32_t) * (size_t)drop_words));
+            engine->drop_words = drop_words;
+        }
+        BGO_CUDA(cudaMemsetAsync(engine->d_drop, 0, sizeof(uint32_t) * (size_t)drop_words, s));
+        engine->last_listable = 1;
+    } else {
+        // a rescan continues the counts; only the error word starts at zero
+        BGO_CUDA(cudaMemsetAsync(engine->d_counter + 2, 0, sizeof(unsigned long long), s));
+    }
     engine->launched = 1;
     if (plan->n_families == 0) return BGO_OK;
     ScanParams p{};
+    p.drop_bits = engine->d_drop;
+    p.drop_base1 = gran[0];
     p.max_mm = max_mismatches;
     p.fams = plan->d_fams;
     p.guides = plan->d_guides;
@@ -745,6 +787,7 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
     p.cap = engine->cap;
     p.counter = engine->d_counter;
     const int64_t max_grid = (int64_t)engine->sm_count * blocks_per_sm();
+    if (mode == 0 || mode == 1 || mode == 3) engine->last_listable = 0;
     if (mode == 0) {
         for (int i = 0; i < n_strands; ++i) {
             fill_strand(p.strand[0], strands[i], n_encoded[i], i);
@@ -795,6 +838,12 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
             q.n_strands = n_strands;
             q.tiles_total = q.strand[0].n_tiles + (n_strands > 1 ? q.strand[1].n_tiles : 0);
             if (q.tiles_total == 0) return BGO_OK;
+            if (engine->rescan) {
+                const int li = chunk == 1024 ? 0 : 1;
+                q.chunk_list = engine->rescan_list[li];
+                q.n_list = engine->rescan_n[li];
+                if (q.n_list == 0) return BGO_OK;
+            }
             q.fam_begin = fb;
             q.fam_end = fe;
             const int rc = launch_seed_kernel(q, sa, engine->sm_count, chunk, minb, t.tolerance,
@@ -821,6 +870,12 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
                 if (q.tiles_total >= (1ll << 31)) {
                     set_error("prefiltered segment index: more than 2^31 chunks");
                     return BGO_ERR_ARG;
+                }
+                if (engine->rescan) {
+                    const int li = chunk == 4096 ? 2 : 1;
+                    q.chunk_list = engine->rescan_list[li];
+                    q.n_list = engine->rescan_n[li];
+                    if (q.n_list == 0) return BGO_OK;
                 }
                 q.fam_begin = g0;
                 q.fam_end = g1;
@@ -861,6 +916,7 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
             return BGO_OK;
         };
         auto every_guide_launch = [&](int fb, int fe) -> int {
+            engine->last_listable = 0;
             ScanParams q = p;
             for (int i = 0; i < n_strands; ++i) fill_strand(q.strand[i], strands[i], n_encoded[i], i);
             q.n_strands = n_strands;
@@ -896,6 +952,7 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
             if (rc != BGO_OK) return rc;
         }
     } else {
+        engine->last_listable = 0;
         for (int i = 0; i < n_strands; ++i) fill_strand(p.strand[i], strands[i], n_encoded[i], i);
         p.n_strands = n_strands;
         p.tiles_total = p.strand[0].n_tiles + (n_strands > 1 ? p.strand[1].n_tiles : 0);
@@ -922,7 +979,153 @@ extern "C" int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan,
     cudaStream_t s = (cudaStream_t)stream;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     BGO_CUDA(cudaStreamIsCapturing(s, &cap));
-    if (cap == cudaStreamCaptureStatusNone) BGO_CUDA(cudaEventRecord(plan->done, s));
+    if (cap == cudaStreamCaptureStatusNone) {
+        BGO_CUDA(cudaEventRecord(plan->done, s));
+        BGO_CUDA(cudaEventRecord(engine->keys_done, s));
+    }
+    return BGO_OK;
+}
+
+// Keys of granules whose keys were partly dropped are removed (their
+// granules are scanned again); the others are appended to dst.
+__global__ void drop_compact_kernel(const uint64_t *__restrict__ src, int64_t n,
+                                    const uint32_t *__restrict__ bits, int64_t base1,
+                                    uint64_t *__restrict__ dst, unsigned long long *counter) {
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        const int64_t i = i0 + threadIdx.x;
+        bool keep = false;
+        uint64_t k = 0;
+        if (i < n) {
+            k = src[i];
+            const int64_t pos = (int64_t)((k >> 6) & 0xFFFFFFFFull);
+            const int64_t g = (((k >> 38) & 1ull) ? base1 : 0) + pos / kDropGranule;
+            keep = !((bits[g >> 5] >> (g & 31)) & 1u);
+        }
+        const unsigned bal = __ballot_sync(0xFFFFFFFFu, keep);
+        unsigned long long at = 0;
+        if (lane == 0 && bal) at = atomicAdd(counter, (unsigned long long)__popc(bal));
+        at = __shfl_sync(0xFFFFFFFFu, at, 0);
+        if (keep) dst[at + __popc(bal & ((1u << lane) - 1u))] = k;
+    }
+}
+
+extern "C" int bgo_scan_complete(bgo_engine *engine, const bgo_plan *plan,
+                                 const bgo_genome *const *strands, const int32_t *n_encoded,
+                                 int32_t n_strands, int32_t max_mismatches, int32_t mode,
+                                 void *stream, int64_t *n_hits) {
+    if (!engine || !plan || !strands || !n_encoded || !n_hits || n_strands < 1 || n_strands > 2) {
+        set_error("bgo_scan_complete: invalid argument");
+        return BGO_ERR_ARG;
+    }
+    if (!engine->launched) {
+        set_error("bgo_scan_complete: no launch to complete");
+        return BGO_ERR_STATE;
+    }
+    BGO_CUDA(cudaSetDevice(engine->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long cnt[3] = {0, 0, 0};
+    BGO_CUDA(cudaMemcpyAsync(cnt, engine->d_counter, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+    BGO_CUDA(cudaStreamSynchronize(s));
+    engine->d2h_bytes += (int64_t)sizeof(cnt);
+    if (cnt[2] & 1u) {
+        set_error("bgo_scan_complete: a chunk copy of the last scan did not complete in time");
+        return BGO_ERR_TIMEOUT;
+    }
+    const int64_t n = (int64_t)cnt[0];
+    *n_hits = n;
+    if (n <= engine->cap) return BGO_OK;
+    if (!engine->last_listable) {
+        // a form that scans tiles without a chunk list: grow and scan again
+        int rc = bgo_engine_reserve(engine, n);
+        if (rc == BGO_OK)
+            rc = bgo_scan_launch(engine, plan, strands, n_encoded, n_strands, max_mismatches, mode,
+                                 stream);
+        if (rc != BGO_OK) return rc;
+        BGO_CUDA(cudaMemcpyAsync(cnt, engine->d_counter, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+        BGO_CUDA(cudaStreamSynchronize(s));
+        *n_hits = (int64_t)cnt[0];
+        return BGO_OK;
+    }
+    // granules with dropped keys, and the chunks of each chunk length that
+    // cover them
+    int64_t gran[2] = {0, 0};
+    for (int i = 0; i < n_strands; ++i)
+        gran[i] = std::max<int64_t>(0, ceil_div(strands[i]->total_bp - kSiteSpan, kDropGranule));
+    const int64_t words = (gran[0] + gran[1]) / 32 + 1;
+    std::vector<uint32_t> bits((size_t)words);
+    BGO_CUDA(cudaMemcpyAsync(bits.data(), engine->d_drop, sizeof(uint32_t) * (size_t)words,
+                             cudaMemcpyDeviceToHost, s));
+    BGO_CUDA(cudaStreamSynchronize(s));
+    engine->d2h_bytes += (int64_t)(sizeof(uint32_t) * (size_t)words);
+    const int lens[3] = {1024, 2048, 4096};
+    std::vector<uint32_t> lists[3];
+    for (int64_t g = 0; g < gran[0] + gran[1]; ++g) {
+        if (!((bits[(size_t)(g >> 5)] >> (g & 31)) & 1u)) continue;
+        const int st = g >= gran[0] ? 1 : 0;
+        const int64_t lg = g - (st ? gran[0] : 0);
+        for (int li = 0; li < 3; ++li) {
+            const int per = (int)(kDropGranule / lens[li]);
+            const int64_t tiles = seed_tiles_for(strands[st]->total_bp, lens[li]);
+            const int64_t base = st ? seed_tiles_for(strands[0]->total_bp, lens[li]) : 0;
+            for (int k = 0; k < per; ++k) {
+                const int64_t c = lg * per + k;
+                if (c < tiles) lists[li].push_back((uint32_t)(base + c));
+            }
+        }
+    }
+    size_t list_words = 0;
+    for (auto &l : lists) list_words += l.size();
+    uint32_t *d_lists = nullptr;
+    BGO_CUDA(pool_alloc(engine->device, (void **)&d_lists, sizeof(uint32_t) * (list_words + 1)));
+    size_t at = 0;
+    for (int li = 0; li < 3; ++li) {
+        if (!lists[li].empty())
+            BGO_CUDA(cudaMemcpyAsync(d_lists + at, lists[li].data(),
+                                     sizeof(uint32_t) * lists[li].size(), cudaMemcpyHostToDevice, s));
+        engine->rescan_list[li] = d_lists + at;
+        engine->rescan_n[li] = (int64_t)lists[li].size();
+        at += lists[li].size();
+    }
+    engine->h2d_bytes += (int64_t)(sizeof(uint32_t) * list_words);
+    // a buffer for every hit; the kept keys of the old one move into it
+    uint64_t *keys = nullptr;
+    BGO_CUDA(pool_alloc(engine->device, (void **)&keys, sizeof(uint64_t) * (size_t)n));
+    BGO_CUDA(cudaMemsetAsync(engine->d_counter, 0, sizeof(unsigned long long), s));
+    const int64_t old_n = engine->cap;
+    drop_compact_kernel<<<(unsigned)std::min<int64_t>(ceil_div(old_n, 256), 8L * engine->sm_count),
+                          256, 0, s>>>(engine->d_keys, old_n, engine->d_drop, gran[0], keys,
+                                       engine->d_counter);
+    BGO_CUDA(cudaGetLastError());
+    BGO_CUDA(pool_free_after(engine->device, engine->d_keys, s));
+    engine->d_keys = keys;
+    engine->cap = n;
+    engine->keys_gen++;
+    // scan the listed chunks again, appending to the compacted keys
+    engine->rescan = 1;
+    int rc = bgo_scan_launch(engine, plan, strands, n_encoded, n_strands, max_mismatches, mode,
+                             stream);
+    engine->rescan = 0;
+    for (int li = 0; li < 3; ++li) {
+        engine->rescan_list[li] = nullptr;
+        engine->rescan_n[li] = 0;
+    }
+    cudaError_t fe = pool_free_after(engine->device, d_lists, s);
+    if (rc != BGO_OK) return rc;
+    BGO_CUDA(fe);
+    BGO_CUDA(cudaMemcpyAsync(cnt, engine->d_counter, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+    BGO_CUDA(cudaStreamSynchronize(s));
+    if (cnt[2] & 1u) {
+        set_error("bgo_scan_complete: a chunk copy of the rescan did not complete in time");
+        return BGO_ERR_TIMEOUT;
+    }
+    if ((int64_t)cnt[0] != n) {
+        set_error("bgo_scan_complete: the rescan of the dropped granules found " +
+                  std::to_string(cnt[0]) + " keys in all, not " + std::to_string(n));
+        return BGO_ERR_STATE;
+    }
+    *n_hits = n;
     return BGO_OK;
 }
 
@@ -1057,6 +1260,7 @@ extern "C" int bgo_graph_launch(bgo_graph *g, void *stream) {
     }
     BGO_CUDA(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
     BGO_CUDA(cudaEventRecord(g->plan->done, (cudaStream_t)stream));
+    BGO_CUDA(cudaEventRecord(g->engine->keys_done, (cudaStream_t)stream));
     g->engine->launched = 1;
     g->engine->launches += g->launches_per_replay;
     return BGO_OK;

@@ -79,7 +79,7 @@ __device__ __noinline__ void finish_candidate(const ScanParams &p, uint32_t m, i
     if (mmf > K) return;
     const uint32_t row = __ldg(&p.guides[gbeg + idx].row);
     semit(((uint64_t)row << 39) | (slot << 38) | (pos << 6) | (uint64_t)mmf, p.keys, p.cap,
-          p.counter);
+          p.counter, p.drop_bits, p.drop_base1);
 }
 
 // CTA shapes by MINB: 3 or 4 CTAs of 256 threads per SM; or one CTA per SM
@@ -147,12 +147,18 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, SeedCta<MINB>::kPerSm
         }
     };
     uint32_t cand = 0;
-    const int64_t c_first = (int64_t)blockIdx.x * WARPS + warp;
-    if (c_first < n_chunks) issue(c_first, 0);
+    // the chunks to scan: all of them, or a rescan's list
+    const int64_t n_items = p.chunk_list ? p.n_list : n_chunks;
+    auto chunk_at = [&](int64_t i) -> int64_t {
+        return p.chunk_list ? (int64_t)p.chunk_list[i] : i;
+    };
+    const int64_t i_first = (int64_t)blockIdx.x * WARPS + warp;
+    if (i_first < n_items) issue(chunk_at(i_first), 0);
     cp_async_commit();
     int buf = 0;
-    for (int64_t c = c_first; c < n_chunks; c += stride, buf ^= 1) {
-        if (c + stride < n_chunks) issue(c + stride, buf ^ 1);
+    for (int64_t it = i_first; it < n_items; it += stride, buf ^= 1) {
+        const int64_t c = chunk_at(it);
+        if (it + stride < n_items) issue(chunk_at(it + stride), buf ^ 1);
         cp_async_commit();
         cp_async_wait<1>();  // this chunk's copies are done; the next one is in flight
         __syncwarp();
@@ -415,7 +421,8 @@ static int launch_k(const ScanParams &p, const SeedArgs &sa, int sm_count, int c
     if (per_sm < 1) per_sm = 1;
     if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
     constexpr int WARPS = SeedCta<MINB>::kWarps;
-    const int64_t blocks_needed = (p.tiles_total + WARPS - 1) / WARPS;
+    const int64_t items = p.chunk_list ? p.n_list : p.tiles_total;
+    const int64_t blocks_needed = (items + WARPS - 1) / WARPS;
     const int64_t grid = std::min<int64_t>(blocks_needed, (int64_t)sm_count * per_sm);
     scan_seed_kernel<K, TOL, INLINE, WALK, CH, MINB>
         <<<(unsigned)grid, SeedCta<MINB>::kThreads, smem, s>>>(p, sa);

@@ -1,5 +1,7 @@
-// Seeded synthetic genomes in the reference .npz layout, generated on the
-// device, and a probe of the integer pipes' throughput.
+// Tools library (libbgo_tools.so, include/bgo_tools.h), not the product:
+// seeded synthetic genomes in the reference .npz layout, generated on the
+// device for the benchmarks and tests, and a probe of the integer pipes'
+// throughput for the benchmark's roofline figures.
 //
 // Genome generator: every base is a pure function of (seed, forward position):
 // byte (p & 7) of splitmix64(seed * 0x9E3779B97F4A7C15 + (p >> 3)) (the
@@ -20,7 +22,8 @@
 #include <cstring>
 #include <vector>
 
-#include "bgo_internal.cuh"
+#include "../bgo_internal.cuh"
+#include "bgo_tools.h"
 
 namespace bgo {
 

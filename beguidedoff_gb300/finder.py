@@ -400,10 +400,9 @@ class beguidedoff:
                 n_rows += len(pairs)
                 parts.append(rows)
                 owners.append([g.guide_id for _, g, _ in pairs])
-            n = eng.hit_count(stream)
-            if n > eng.info()["hit_capacity"]:
-                eng.reserve(n)
-                eng.launch(plan, self._strands, ne, max_mismatches, mode, stream)
+            # every hit in the buffer: an overflowing scan rescans only the
+            # granules whose keys did not fit
+            n = eng.complete(plan, self._strands, ne, max_mismatches, mode, stream)
             t2 = time.perf_counter()
             # this batch's own record (batches of several serving slots run
             # concurrently; last_batch only ever receives a finished record)

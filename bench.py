@@ -74,6 +74,133 @@ def make_workload(genome_bp, n_guides, seed=2):
     return lens, blocks, guides
 
 
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _splitmix64(x):
+    """SplitMix64 finaliser (Steele, Lea and Flood 2014) on uint64 arrays,
+    the generator of the device synthetic genome (bgo_synth_genome)."""
+    with np.errstate(over="ignore"):
+        z = x + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def _cpu_bases(pos, seed, thresholds, total, repeats, fam_seq):
+    """Base codes (0-3) of forward positions `pos` (int64), the device
+    generator's pure function of (seed, position), without N."""
+    u = pos.astype(np.uint64)
+    lo, hi = int(pos.min()), int(pos.max()) + 1
+    if hi - lo <= 2 * pos.size:
+        # one hash per 8 positions over the covered range, read back as bytes
+        w0 = lo >> 3
+        ws = np.arange(w0, ((hi - 1) >> 3) + 1, dtype=np.uint64)
+        with np.errstate(over="ignore"):
+            h = _splitmix64(np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15) + ws)
+        b8 = h.astype("<u8").view(np.uint8)[pos - 8 * w0]
+    else:
+        with np.errstate(over="ignore"):
+            h = _splitmix64(np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15) + (u >> np.uint64(3)))
+        b8 = ((h >> (np.uint64(8) * (u & np.uint64(7)))) & np.uint64(0xFF)).astype(np.uint8)
+    t0, t1, t2 = (np.uint8(t) for t in thresholds)
+    out = np.where(b8 < t0, 0, np.where(b8 < t1, 1, np.where(b8 < t2, 2, 3))).astype(np.uint8)
+    if repeats:
+        n_copies, flen = int(repeats["n_copies"]), int(repeats["family_len"])
+        region = total // n_copies
+        rseed = np.uint64(int(repeats.get("seed", seed)))
+        div16 = np.uint64(int(round(float(repeats["divergence"]) * 65536)))
+        r = pos // region
+        with np.errstate(over="ignore"):
+            hr = _splitmix64(rseed * np.uint64(0xD6E8FEB86659FD93) + r.astype(np.uint64))
+        start = r * region + (hr % np.uint64(region - flen + 1)).astype(np.int64)
+        i = pos - start
+        inside = (r < n_copies) & (i >= 0) & (i < flen)
+        if inside.any():
+            ii, hh, pp = i[inside], hr[inside], u[inside]
+            f = (((hh >> np.uint64(32)) & np.uint64(0xFFFFFF)) %
+                 np.uint64(int(repeats["n_families"]))).astype(np.int64)
+            rev = (hh >> np.uint64(63)) == 1
+            fwd_b = fam_seq[f * flen + ii]
+            rev_b = 3 - fam_seq[f * flen + flen - 1 - ii]
+            b = np.where(rev, rev_b, fwd_b).astype(np.uint64)
+            with np.errstate(over="ignore"):
+                h2 = _splitmix64((rseed ^ np.uint64(0xA0761D6478BD642F)) + pp)
+            sub = (h2 & np.uint64(0xFFFF)) < div16
+            b = np.where(sub, (b + np.uint64(1) + (h2 >> np.uint64(16)) % np.uint64(3)) &
+                         np.uint64(3), b)
+            out[inside] = b.astype(np.uint8)
+    return out
+
+
+def cpu_repeat_families(repeats):
+    """The repeat family sequences bgo_synth_genome_repeats inserts (strings)."""
+    n = int(repeats["n_families"]) * int(repeats["family_len"])
+    with np.errstate(over="ignore"):
+        codes = (_splitmix64(np.uint64(int(repeats["seed"])) * np.uint64(0x9E3779B97F4A7C15) +
+                             np.uint64(0x5851F42D4C957F2D) + np.arange(n, dtype=np.uint64))
+                 >> np.uint64(62)).astype(np.int64)
+    flen = int(repeats["family_len"])
+    return ["".join("ACGT"[c] for c in codes[i:i + flen]) for i in range(0, n, flen)]
+
+
+def cpu_synth_prefix(seed, lens, blocks, thresholds, n_pos, repeats=None):
+    """The first n_pos positions of both strand arrays of the synthetic genome
+    (bit-identical to bgo_synth_genome), built on the host with numpy: packed
+    forward and reverse-complement words and their little-endian N masks, as
+    the oracle scans them.  Only the reference arm uses it, so that the CPU
+    baseline loads no product code."""
+    lens = np.asarray(lens, dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(lens)[:-1]])
+    total = int(lens.sum())
+    n_pos = min(int(n_pos), total)
+    bs = np.array([b[0] for b in blocks], dtype=np.int64)
+    be = np.array([b[1] for b in blocks], dtype=np.int64)
+    fam_seq = None
+    if repeats:
+        n = int(repeats["n_families"]) * int(repeats["family_len"])
+        rseed = np.uint64(int(repeats.get("seed", seed)))
+        with np.errstate(over="ignore"):
+            fam_seq = (_splitmix64(rseed * np.uint64(0x9E3779B97F4A7C15) +
+                                   np.uint64(0x5851F42D4C957F2D) + np.arange(n, dtype=np.uint64))
+                       >> np.uint64(62)).astype(np.int64)
+
+    def is_n(pos):
+        k = np.searchsorted(be, pos, side="right")
+        ok = k < bs.size
+        res = np.zeros(pos.shape, dtype=bool)
+        res[ok] = bs[k[ok]] <= pos[ok]
+        return res
+
+    n_words = (n_pos + 15) // 16
+    fwd = np.zeros(n_words, dtype=np.uint32)
+    rc = np.zeros(n_words, dtype=np.uint32)
+    nm_f = np.zeros((n_pos + 7) // 8 + 16, dtype=np.uint8)
+    nm_r = np.zeros_like(nm_f)
+    step = 1 << 23
+    for a in range(0, n_words * 16, step):
+        q = np.arange(a, min(a + step, n_words * 16), dtype=np.int64)
+        valid = q < total
+        qf = np.minimum(q, total - 1)
+        nf = is_n(qf) & valid
+        bf = np.where(nf | ~valid, 0, _cpu_bases(qf, seed, thresholds, total, repeats, fam_seq))
+        c = np.searchsorted(offs, qf, side="right") - 1
+        src = offs[c] + lens[c] - 1 - (qf - offs[c])
+        nr = is_n(src) & valid
+        br = np.where(~valid, 0, 3 - np.where(nr, 0, _cpu_bases(src, seed, thresholds, total,
+                                                                 repeats, fam_seq)))
+        for arr, b in ((fwd, bf), (rc, br)):
+            w = b.astype(np.uint32).reshape(-1, 16) << (2 * np.arange(16, dtype=np.uint32))
+            arr[a // 16:a // 16 + w.shape[0]] = np.bitwise_or.reduce(w, axis=1)
+        lim = min(q.size, n_pos - a)
+        if lim > 0:
+            for m, nb in ((nm_f, nf), (nm_r, nr)):
+                bits = np.packbits(nb[:lim].astype(np.uint8), bitorder="little")
+                m[a // 8:a // 8 + bits.size] |= bits
+    return {"genome_forward": fwd, "genome_rc": rc, "total_bp": total, "n_pos": n_pos,
+            "_nm_fwd_le": nm_f, "_nm_rc_le": nm_r}
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
 
@@ -261,47 +388,69 @@ def cpu_scan_rate(genome, guides, max_mm, target_s, n_threads=0, budget_bp=None,
     return rate, threads, f"positions [0, {span}) of both strands x {len(guides)} guides", dt
 
 
+REFERENCE_SAMPLE_BP = 32_000_000
+SHIM_RATE_FILE = os.path.join(ROOT, "tests", "golden", "reference_shim_rate.json")
+
+
 def bench_reference(args, ws, rank):
-    """CPU restatement of the reference scan (no compiled reference exists for
-    this path: the reference kernel is Numba-JIT CUDA) on all host cores."""
+    """The reference arm: the CPU restatement of the reference scan
+    (oracle/scan_oracle.c, OpenMP on all host cores; the reference itself has
+    no CPU implementation of this path and its kernel is Numba-JIT CUDA) on a
+    bounded sample of the same workload: positions [0, REFERENCE_SAMPLE_BP) of
+    both strands of the same synthetic genome, built on the host (no product
+    code is loaded).  Each step is one timed scan of that sample."""
     if rank != 0:
         return
-    from beguidedoff_gb300 import _native
+    from oracle import oracle as O
 
     lens, blocks, guides = make_workload(args.genome_bp, args.guides)
     pams = guide_pams(args, len(guides))
-    genome = _native.synth_genome(7, lens, blocks, thresholds=(76, 128, 180),
-                                  device=int(os.environ.get("LOCAL_RANK", "0")),
-                                  repeats=DENSE_REPEATS if args.config == "dense" else None)
+    reps = DENSE_REPEATS if args.config == "dense" else None
+    span = int(min(REFERENCE_SAMPLE_BP, int(lens.sum()) - 26))
+    t0 = time.perf_counter()
+    g = cpu_synth_prefix(7, lens, blocks, (76, 128, 180), span + 64, repeats=reps)
+    t_synth = time.perf_counter() - t0
     if args.config == "dense":
-        guides = dense_guides(genome["repeat_families"], pams)
+        guides = dense_guides(cpu_repeat_families(reps), pams)
     guides, pams = select_families(args, guides, pams)
     args.guides = len(guides)
-    from beguidedoff_gb300.finder import prepare_n_masks
+    gv, pm, pl, p3 = plan_arrays(guides, pams)
+    tb = int(lens.sum())
+    threads = O.max_threads()
 
-    genome["_nm_fwd_le"], genome["_nm_rc_le"] = prepare_n_masks(genome)
-    per_step = max(1.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    def step():
+        t = time.perf_counter()
+        for arr, nm, ne in ((g["genome_forward"], g["_nm_fwd_le"], 0),
+                            (g["genome_rc"], g["_nm_rc_le"], 3)):
+            O.scan_strand(arr, tb, nm, gv, pm, pl, p3, args.max_mm, ne, 0, span, 0)
+        return time.perf_counter() - t
+
     for _ in range(args.warmup):
-        cpu_scan_rate(genome, guides, args.max_mm, per_step / 4, pams=pams)
-    rates, sample, threads = [], "", 0
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        r, threads, sample, _dt = cpu_scan_rate(genome, guides, args.max_mm, per_step, pams=pams)
-        rates.append(r)
-    wall = time.perf_counter() - t0
-    value = statistics.median(rates)
-    comps = args.guides * 2 * (int(lens.sum()) - 26)
+        step()
+    times = [step() for _ in range(args.steps)]
+    sec = statistics.median(times)
+    value = len(guides) * 2 * span / sec
+    sample = (f"positions [0, {span}) of both strands x {len(guides)} guides per step, "
+              f"the same synthetic genome built on the host")
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * comps / value, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": workload_config(args, lens),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic", "config": workload_config(args, lens),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": sample + " per step (oracle/scan_oracle.c, OpenMP)"},
+                         "sample": sample + " (oracle/scan_oracle.c, OpenMP)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "wall_s": wall,
+        "step_s": times, "synth_s": t_synth,
     }
+    # the reference's own kernel body, run literally on one core through the
+    # test-only CPU stand-ins (tests/golden/reference_shim_rate.py); it needs
+    # the reference checkout, so it is measured in the build container and
+    # read here
+    try:
+        shim = json.load(open(SHIM_RATE_FILE))
+        out["cpu_baseline_reference_shim"] = dict(shim, kind="reference-shim")
+    except (OSError, ValueError):
+        pass
     print(json.dumps(out))
 
 
@@ -316,7 +465,7 @@ def workload_config(args, lens):
                 f"scan + device epilogue (score ranks, window filter, below-threshold counts, "
                 f"top-{3} candidates)")
         return {"workload": name, "genome_bp": int(lens.sum()), "guides": args.guides,
-                "pam": "mixed", "max_mismatches": args.max_mm, "scan_mode": args.mode,
+                "pam": "mixed", "max_mismatches": args.max_mm, "scan_mode": args.mode_requested,
                 "repeats": DENSE_REPEATS,
                 "l2": "inputs larger than L2 (bit planes of both strands ~2.3 GB)"}
     if args.config == "mixed":
@@ -333,7 +482,7 @@ def workload_config(args, lens):
     return {
         "workload": name,
         "genome_bp": int(lens.sum()), "guides": args.guides, "pam": pam,
-        "max_mismatches": args.max_mm, "scan_mode": args.mode,
+        "max_mismatches": args.max_mm, "scan_mode": args.mode_requested,
         "l2": "inputs larger than L2 (bit planes of both strands ~2.3 GB)",
     }
 
@@ -794,6 +943,7 @@ def main():
                     help="plain: 100 NGG guides, <=4 mm; mixed: 400 mixed-PAM guides, <=5 mm; "
                          "dense: repeat-family genome, 1000 mixed guides, <=6 mm")
     args = ap.parse_args()
+    args.mode_requested = args.mode
     if args.mode != "auto":
         args.mode = int(args.mode)
     if args.warmup < 3:

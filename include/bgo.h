@@ -143,6 +143,22 @@ int bgo_scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genome *
 int bgo_scan_collect(bgo_engine *engine, uint64_t *keys, int64_t capacity, int64_t *n_hits,
                      void *stream);
 
+/*
+ * Completes the last scan of `engine` (after bgo_scan_launch of the same
+ * plan, strands and parameters, on the same stream) so that the hit buffer
+ * holds every hit: *n_hits = the exact count.  When the scan overflowed the
+ * buffer, the keys that did not fit have marked their 4,096-position granules;
+ * the engine grows the buffer (without synchronising the device), keeps the
+ * keys of the other granules and scans only the marked granules again (the
+ * segment-index and prefiltered forms take a chunk list; the other forms scan
+ * everything once more).  The reference's counterpart is the escalating
+ * whole-genome re-scan of overflowed guides (beguidedoff/finder.py:568-638,
+ * ceiling :100-116); here no hit is ever truncated.
+ */
+int bgo_scan_complete(bgo_engine *engine, const bgo_plan *plan, const bgo_genome *const *strands,
+                      const int32_t *n_encoded, int32_t n_strands, int32_t max_mismatches,
+                      int32_t mode, void *stream, int64_t *n_hits);
+
 /* After the last launch completed: number of (PAM-passing position, guide
  * row) pairs whose mismatches were counted.  No reference counterpart: it is
  * the work figure of the roofline. */
@@ -336,14 +352,20 @@ int bgo_engine_transfer(const bgo_engine *engine, int64_t *h2d_bytes, int64_t *d
  * The scan for callers that cannot allocate device memory: programs whose own
  * allocator already owns the GPU's memory, and latency-critical loops where a
  * cudaMalloc/cudaFree would synchronise the device.  No counterpart in the
- * reference.  It allocates nothing (device or host): its guide tables,
- * counters and a key buffer live in one static device array of about 8.1 MB
- * that every GPU loading this library reserves until the process exits.  The
- * first call on a device looks that array's address up (make it before any
- * stream capture); calls whose work overlaps on the GPU share the array and
- * race, so serialise them.  Limits: n_guides <= BGO_NOALLOC_MAX_GUIDES
- * (larger values return BGO_ERR_ARG), at most BGO_NOALLOC_MAX_HITS hits per
- * call (more return BGO_ERR_OOM with the exact count in *n_hits).
+ * reference.  It allocates no device memory: its guide tables, counters
+ * and a key buffer live in one static device array of about 8.1 MB that every
+ * GPU loading this library reserves until the process exits.  On the host it
+ * works in static tables (no heap, small stack); only a failing call
+ * allocates, to record its error message.  The first call on a device looks
+ * the device array's address up (make it before any stream capture); calls
+ * whose work overlaps on the GPU share the array and race, so serialise them
+ * (concurrent host threads are serialised by the library).  Limits: n_guides
+ * <= BGO_NOALLOC_MAX_GUIDES (larger values return BGO_ERR_ARG), at most
+ * BGO_NOALLOC_MAX_HITS hits per call (more return BGO_ERR_OOM with the exact
+ * count in *n_hits).  A call whose hits fit the static buffer but not
+ * `capacity` returns BGO_OK with the exact count and leaves `keys` untouched:
+ * compare *n_hits with capacity.  It runs the plain compare-every-guide scan
+ * (scan mode 1), the form that needs no index memory.
  * Inputs and outputs are the caller's: strands as for bgo_scan_launch, guide
  * rows as for bgo_plan_create (host arrays); on success *n_hits is the exact
  * hit count and, when it is <= capacity, `keys` (host) receives all hit keys in
@@ -368,53 +390,6 @@ int bgo_scan_noalloc(const bgo_genome *const *strands, const int32_t *n_encoded,
 int bgo_encode_genome(const uint8_t *seq, const int64_t *chrom_lengths, int32_t n_chroms,
                       int device, uint32_t *fwd_out, uint32_t *rc_out, uint8_t *n_mask_big_out);
 
-/*
- * Seeded synthetic genome in the reference .npz layout (what
- * beguidedoff/genome_converter.py:15-108 writes for the equivalent FASTA):
- * chromosomes of the given lengths concatenated, bases drawn per position from
- * cumulative byte thresholds (A below t[0], C below t[1], G below t[2], else T),
- * N in the sorted disjoint half-open blocks [n_starts[i], n_ends[i]).
- * Outputs (host): fwd_out / rc_out ceil(total/16) words, n_mask_big_out
- * ceil(total/8) bytes in np.packbits (big) bit order.  No reference
- * counterpart: it stands in for the real assemblies the benchmarks used.
- */
-int bgo_synth_genome(uint64_t seed, const int64_t *chrom_lengths, int32_t n_chroms,
-                     const int64_t *n_starts, const int64_t *n_ends, int64_t n_blocks,
-                     const uint8_t *thresholds, int device, uint32_t *fwd_out, uint32_t *rc_out,
-                     uint8_t *n_mask_big_out);
-
-/*
- * Repeat families inserted by bgo_synth_genome_repeats: the genome is cut
- * into n_copies equal regions; region r holds one copy of a seeded family at a
- * seeded offset and orientation, each base substituted with probability
- * divergence_65536 / 65536.  Families are uniform random ACGT of family_len bp.
- */
-typedef struct bgo_repeat_spec {
-    int32_t n_families;
-    int32_t family_len;
-    int64_t n_copies;
-    uint32_t divergence_65536;
-    uint32_t reserved;
-    uint64_t seed;
-} bgo_repeat_spec;
-
-/*
- * bgo_synth_genome with repeat families (the hit-dense workload).
- * families_out receives n_families * family_len base codes (0-3 = ACGT).
- */
-int bgo_synth_genome_repeats(uint64_t seed, const int64_t *chrom_lengths, int32_t n_chroms,
-                             const int64_t *n_starts, const int64_t *n_ends, int64_t n_blocks,
-                             const uint8_t *thresholds, const bgo_repeat_spec *repeats,
-                             uint8_t *families_out, int device, uint32_t *fwd_out,
-                             uint32_t *rc_out, uint8_t *n_mask_big_out);
-
-/*
- * Measured throughput (Gop/s) of one integer instruction on `device`:
- * op 0 = LOP3, 1 = POPC, 2 = 32-bit add.  Independent chains, 8 CTAs of 256
- * threads per SM, best of 3 timed launches.  No reference counterpart: it is
- * the roofline denominator of the scan kernels.
- */
-int bgo_probe_int_throughput(int device, int op, double *gops_per_s);
 
 #ifdef __cplusplus
 }

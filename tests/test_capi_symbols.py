@@ -1,5 +1,6 @@
 """The C-ABI library builds here, loads, and exports every function that
-include/bgo.h declares (no device calls: this runs without a GPU)."""
+include/bgo.h declares; the tools library exports those of include/bgo_tools.h
+(no device calls: this runs without a GPU)."""
 import ctypes
 import os
 import re
@@ -11,13 +12,14 @@ from beguidedoff_gb300 import _native, build
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _declared():
-    txt = open(os.path.join(ROOT, "include", "bgo.h")).read()
+def _declared(header="bgo.h"):
+    txt = open(os.path.join(ROOT, "include", header)).read()
     return sorted(set(re.findall(r"^int (bgo_\w+)\(", txt, flags=re.M)))
 
 
 def test_header_and_binding_agree():
     assert _declared() == sorted(_native.EXPORTED)
+    assert _declared("bgo_tools.h") == sorted(_native.TOOLS_EXPORTED)
 
 
 def test_library_exports_every_declared_symbol():
@@ -28,6 +30,10 @@ def test_library_exports_every_declared_symbol():
     lib = ctypes.CDLL(path)
     for name in _declared():
         assert hasattr(lib, name), name
+    tools = ctypes.CDLL(build.TOOLS_PATH)
+    for name in _declared("bgo_tools.h"):
+        assert hasattr(tools, name), name
+        assert not hasattr(lib, name), f"{name} is a tool, not in the product library"
     lib.bgo_version.restype = ctypes.c_int
     assert lib.bgo_version() >= 100
     buf = ctypes.create_string_buffer(64)

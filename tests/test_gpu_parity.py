@@ -10,6 +10,7 @@ from _keys import oracle_keys, table_rows
 from beguidedoff_gb300 import _native, build
 from beguidedoff_gb300 import cuda_search as CS
 from beguidedoff_gb300.finder import beguidedoff, prepare_n_masks
+from beguidedoff_gb300.genome_converter import encode_chromosomes
 from beguidedoff_gb300.types import GuideInput
 from oracle import oracle as O
 
@@ -267,6 +268,60 @@ def test_prefilter_headline_shape_equals_oracle(k, chunk):
         finally:
             g.close()
         plan.close()
+    finally:
+        f.close()
+
+
+@pytest.mark.parametrize("tune", [(2048, 0, 0, 0, 0, 1, 0, 0, 1), (4096, 0, 0, 0, 0, 1, 0, 0, 1),
+                                  (0, 0, 0, 0, 1, 1), (0, 0, 0, 0, 3, 0), None])
+def test_overflow_rescans_only_dropped_granules(tune):
+    """More hits than a fresh engine's buffer holds (1,048,576 keys): poly-A
+    and poly-T runs hit at every position on one strand each.  After
+    bgo_scan_complete the buffer holds exactly the oracle's keys; with the
+    chunk-listed forms (segment index, prefiltered) the rescan covered only
+    the granules whose keys were dropped (fewer pairs than a second full scan),
+    and the other forms (tune None: the plain form) scan everything again."""
+    rng = np.random.default_rng(404)
+    bases = np.frombuffer(b"ACGT", dtype=np.uint8)
+    c1 = bytearray(rng.choice(bases, 2_500_000).tobytes())
+    c1[200_000:1_000_000] = b"A" * 800_000
+    c2 = bytearray(rng.choice(bases, 1_000_003).tobytes())
+    c2[300_000:700_000] = b"T" * 400_000
+    genome = encode_chromosomes([("chrA", bytes(c1)), ("chrB", bytes(c2))])
+    seqs, pams = ["A" * 20, "T" * 20, "ACGTACGTACGTACGTACGT"], ["NNN", "NRG", "NGG"]
+    exp = oracle_keys(genome, seqs, pams, 2)
+    assert exp.size > (1 << 20)
+    f = beguidedoff(None, max_mismatches=2, genome_data=genome)
+    try:
+        eng = _native.Engine(0)
+        plan = f._plan(seqs, pams, engine=eng)
+        mode = 2 if tune is not None else 0
+        if tune is not None:
+            plan.set_tuning(*tune)
+        # one scan without overflow for the pair count of a full scan
+        big = _native.Engine(0)
+        big.reserve(exp.size)
+        plan2 = f._plan(seqs, pams, engine=big)
+        if tune is not None:
+            plan2.set_tuning(*tune)
+        big.launch(plan2, f._strands, [0, 3], 2, mode)
+        assert big.complete(plan2, f._strands, [0, 3], 2, mode) == exp.size
+        full_pairs = big.pairs_evaluated()
+        plan2.close()
+        big.close()
+        assert eng.info()["hit_capacity"] < exp.size
+        eng.launch(plan, f._strands, [0, 3], 2, mode)
+        first = eng.hit_count()
+        assert first == exp.size
+        n = eng.complete(plan, f._strands, [0, 3], 2, mode)
+        assert n == exp.size
+        got_n, keys = eng.collect()
+        assert got_n == exp.size and np.array_equal(keys, exp)
+        pairs = eng.pairs_evaluated()
+        if tune is not None:
+            assert full_pairs < pairs < 2 * full_pairs, (full_pairs, pairs)
+        plan.close()
+        eng.close()
     finally:
         f.close()
 

@@ -55,6 +55,26 @@ def test_pam_known_answers():
     assert len(groups[("NGG", "3prime")]) == 2 and len(groups[("NNGRRT", "3prime")]) == 1
 
 
+def test_pam_matches_at_position_against_allowed_sets():
+    """The per-base PAM test of the reference's pam.py: every IUPAC code at
+    every base, a PAM that runs past the genome's end, and NNGRRT windows."""
+    codes = "ACGTRYSWKMBDHVN"
+    genome = np.array([0, 1, 2, 3], dtype=np.uint8)   # A C G T
+    for c in codes:
+        m = P.encode_pam_mask(c)
+        for pos in range(4):
+            exp = "ACGT"[genome[pos]] in {"A": "A", "C": "C", "G": "G", "T": "T", "R": "AG",
+                                          "Y": "CT", "S": "CG", "W": "AT", "K": "GT",
+                                          "M": "AC", "B": "CGT", "D": "AGT", "H": "ACT",
+                                          "V": "ACG", "N": "ACGT"}[c]
+            assert P.pam_matches_at_position(genome, pos, m, 1) == exp, (c, pos)
+    assert not P.pam_matches_at_position(genome, 3, P.encode_pam_mask("NN"), 2)
+    g = np.array([1, 1, 2, 0, 2, 3, 0], dtype=np.uint8)   # C C G A G T A
+    m = P.encode_pam_mask("NNGRRT")
+    assert P.pam_matches_at_position(g, 0, m, 6)
+    assert not P.pam_matches_at_position(g, 1, m, 6)
+
+
 def test_cctop_known_answers():
     assert S.calculate_cctop_score([]) == 0.0
     assert abs(S.calculate_cctop_score([20]) - 1.2 ** 20) < 1e-9

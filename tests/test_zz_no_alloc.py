@@ -21,24 +21,28 @@ from beguidedoff_gb300.pam import encode_pam_mask
 pytestmark = pytest.mark.gpu
 
 
-def _rows(rng, n, pams):
-    seqs = ["".join(rng.choice(list("ACGT"), 20)) for _ in range(n)]
-    ps = [pams[i % len(pams)] for i in range(n)]
+def _encode(seqs, ps):
     gv = np.array([encode_guide_64bit(encode_dna(s)) for s in seqs], dtype=np.uint64)
     pm = np.stack([encode_pam_mask(p) for p in ps]).astype(np.uint8)
     pl = np.array([len(p) for p in ps], dtype=np.uint8)
-    return gv, pm, pl, np.ones(n, dtype=np.uint8)
+    return gv, pm, pl, np.ones(len(seqs), dtype=np.uint8)
 
 
-def _noalloc(strands, rows, max_mm, capacity):
+def _rows(rng, n, pams):
+    seqs = ["".join(rng.choice(list("ACGT"), 20)) for _ in range(n)]
+    return _encode(seqs, [pams[i % len(pams)] for i in range(n)])
+
+
+def _noalloc(strands, rows, max_mm, capacity, stream=None, keys=None):
     gv, pm, pl, p3 = rows
     handles = (ctypes.c_void_p * len(strands))(*[s.handle.value for s in strands])
     ne = np.array([0, 3][:len(strands)], dtype=np.int32)
-    keys = np.zeros(capacity, dtype=np.uint64)
+    if keys is None:
+        keys = np.zeros(capacity, dtype=np.uint64)
     n = ctypes.c_int64(-1)
     rc = _native.lib().bgo_scan_noalloc(handles, ne.ctypes.data, len(strands), gv.ctypes.data,
                                         pm.ctypes.data, pl.ctypes.data, p3.ctypes.data, gv.size,
-                                        max_mm, keys.ctypes.data, capacity, ctypes.byref(n), None)
+                                        max_mm, keys.ctypes.data, capacity, ctypes.byref(n), stream)
     return rc, n.value, keys[:max(n.value, 0)]
 
 
@@ -55,6 +59,7 @@ def setup():
     strands = [_native.Strand(g["genome_forward"], g["total_bp"], fwd_nm),
                _native.Strand(g["genome_rc"], g["total_bp"], rc_nm)]
     strands[0].packed = g["genome_forward"]
+    strands[0].genome = g
     eng = _native.Engine(0)
     yield strands, eng
     for s in strands:
@@ -117,3 +122,56 @@ def test_noalloc_limits_are_enforced(setup):
     rc, n2, keys = _noalloc(strands, _rows(np.random.default_rng(5), 60,
                                            ["NGG", "NG", "NNGRRT", "NRN", "TTTV"]), 5, 10 ** 6)
     assert rc == 0 and n2 > 0 and np.all(np.diff(keys.astype(np.int64)) >= 0)
+
+
+def test_noalloc_equals_oracle(setup):
+    """The same keys as the CPU oracle's restatement of the reference kernel,
+    with guides copied from the genome (every row has hits)."""
+    from _keys import oracle_keys
+
+    strands, _ = setup
+    rng = np.random.default_rng(7)
+    starts = rng.integers(0, 2_000_000, 12)
+    from beguidedoff_gb300.encoding import extract_windows
+
+    bases = extract_windows(strands[0].packed, starts, 20)
+    seqs = ["".join("ACGT"[b] for b in row) for row in bases]
+    pams = [["NGG", "NRN", "NNGRRT"][i % 3] for i in range(len(seqs))]
+    exp = oracle_keys(strands[0].genome, seqs, pams, 3)
+    assert exp.size > 0
+    for _ in range(2):
+        rc, n, keys = _noalloc(strands, _encode(seqs, pams), 3, exp.size)
+        assert rc == 0, _native.last_error()
+        assert n == exp.size and np.array_equal(keys, exp)
+
+
+def test_noalloc_short_buffer_empty_call_pamless_rows_and_stream(setup):
+    """A capacity below the hit count returns BGO_OK, the exact count and an
+    untouched key buffer; a call with no guide rows after a call with hits
+    reports 0 hits (the counters are cleared); rows whose PAM length is 0 never
+    match, as in the regular path; a call on a created stream gives the same
+    keys."""
+    strands, eng = setup
+    rng = np.random.default_rng(8)
+    rows = _genome_rows(strands[0].packed, rng, 9, ["NNN"])
+    exp = _regular(eng, strands, rows, 3)
+    assert exp.size > 2
+    sentinel = np.full(exp.size - 1, 7, dtype=np.uint64)
+    rc, n, _ = _noalloc(strands, rows, 3, exp.size - 1, keys=sentinel)
+    assert rc == 0 and n == exp.size and np.all(sentinel == 7)
+    empty = tuple(a[:0] for a in rows)
+    rc, n, _ = _noalloc(strands, empty, 3, 4)
+    assert rc == 0 and n == 0
+    gv, pm, pl, p3 = rows
+    pl0 = pl.copy()
+    pl0[::3] = 0
+    mixed = (gv, pm, pl0, p3)
+    exp0 = _regular(eng, strands, mixed, 3)
+    rc, n, keys = _noalloc(strands, mixed, 3, max(exp0.size, 1))
+    assert rc == 0 and n == exp0.size and np.array_equal(keys, exp0)
+    s = _native.Stream(0)
+    try:
+        rc, n, keys = _noalloc(strands, rows, 3, exp.size, stream=s.handle)
+        assert rc == 0 and n == exp.size and np.array_equal(keys, exp)
+    finally:
+        s.close()
