@@ -330,6 +330,71 @@ def select_families(args, guides, pams):
     return [guides[i] for i in idx], [pams[i] for i in idx]
 
 
+SACAS9_FAMILIES = ("NNGRRT", "NNNRRT")
+
+
+def sacas9_extend(guides, pams, seed=4):
+    """SaCas9-family guides (NNGRRT, NNNRRT) are 21 nt: one more seeded base.
+    The reference compares their first 20 bases and tests the PAM right after
+    them (beguidedoff/encoding.py:70-75, cuda_search.py:239-275)."""
+    rng = np.random.default_rng(seed)
+    return [g + "ACGT"[int(rng.integers(0, 4))] if p in SACAS9_FAMILIES else g
+            for g, p in zip(guides, pams)]
+
+
+def sampled_ranges(lens, blocks, n_ranges, span, seed=5):
+    """Position ranges [lo, hi) of a strand array for the parity check:
+    chromosome junctions, N-block edges and seeded random starts (a quarter,
+    a quarter, the rest)."""
+    lens = np.asarray(lens, dtype=np.int64)
+    total = int(lens.sum())
+    rng = np.random.default_rng(seed)
+    centres = list(np.cumsum(lens)[:-1][: max(1, n_ranges // 4)])
+    edges = [b[0] for b in blocks][:: max(1, len(blocks) // max(1, n_ranges // 4))]
+    centres += edges[: max(1, n_ranges // 4)]
+    while len(centres) < n_ranges:
+        centres.append(int(rng.integers(span, total - span)))
+    out = []
+    for c in sorted(int(x) for x in centres[:n_ranges]):
+        lo = max(0, c - span // 2)
+        hi = min(total - 26, lo + span)
+        if out and lo < out[-1][1]:
+            out[-1] = (out[-1][0], max(out[-1][1], hi))
+        elif hi > lo:
+            out.append((lo, hi))
+    return out
+
+
+def range_parity(genome_arrays, total, guides, pams, max_mm, gpu_keys, ranges, n_threads=0):
+    """The GPU hit keys inside sampled ranges of both strands against the C
+    oracle's rescan of those ranges (the oracle is the checker here, run in
+    the CPU-baseline leg); keys row<<39 | strand<<38 | pos<<6 | mm."""
+    from oracle import oracle as O
+
+    gv = np.array([O.encode_guide(g[:20]) for g in guides], dtype=np.uint64)
+    _, pm, pl, p3 = plan_arrays(guides, pams)
+    gpu_keys = np.asarray(gpu_keys, dtype=np.uint64)
+    g_slot = ((gpu_keys >> np.uint64(38)) & np.uint64(1)).astype(np.int64)
+    g_pos = ((gpu_keys >> np.uint64(6)) & np.uint64(0xFFFFFFFF)).astype(np.int64)
+    exp, got = [], []
+    t0 = time.perf_counter()
+    for slot, (arr, nm, ne) in enumerate(genome_arrays):
+        for lo, hi in ranges:
+            _, keys = O.scan_strand(arr, total, nm, gv, pm, pl, p3, max_mm, ne, lo, hi, n_threads)
+            g, pos, mm = O.split_keys(keys)
+            exp.append((g.astype(np.uint64) << np.uint64(39)) | (np.uint64(slot) << np.uint64(38))
+                       | (pos.astype(np.uint64) << np.uint64(6)) | mm.astype(np.uint64))
+            got.append(gpu_keys[(g_slot == slot) & (g_pos >= lo) & (g_pos < hi)])
+    exp = np.sort(np.concatenate(exp)) if exp else np.zeros(0, dtype=np.uint64)
+    got = np.sort(np.concatenate(got)) if got else np.zeros(0, dtype=np.uint64)
+    return {"ranges": len(ranges) * len(genome_arrays),
+            "bp": int(sum(hi - lo for lo, hi in ranges)) * len(genome_arrays),
+            "keys_in_ranges": int(exp.size), "keys_equal": bool(np.array_equal(exp, got)),
+            "oracle_s": round(time.perf_counter() - t0, 2),
+            "ranges_detail": "chromosome junctions, N-block edges and seeded random starts, "
+                             "both strands"}
+
+
 def dense_guides(families, pams, seed=3):
     """Hit-dense guide set: 30% are 20-mers of a repeat consensus followed by a
     consensus PAM of the guide's family (where the consensus has one), the rest
@@ -412,9 +477,11 @@ def bench_reference(args, ws, rank):
     t_synth = time.perf_counter() - t0
     if args.config == "dense":
         guides = dense_guides(cpu_repeat_families(reps), pams)
+    guides = sacas9_extend(guides, pams)
     guides, pams = select_families(args, guides, pams)
     args.guides = len(guides)
-    gv, pm, pl, p3 = plan_arrays(guides, pams)
+    gv = np.array([O.encode_guide(x[:20]) for x in guides], dtype=np.uint64)
+    _, pm, pl, p3 = plan_arrays(guides, pams)
     tb = int(lens.sum())
     threads = O.max_threads()
 
@@ -487,6 +554,59 @@ def workload_config(args, lens):
     }
 
 
+def speedups(plain, batched_ms):
+    """The batched form's speed-ups over the plain forms of plain_forms()."""
+    out = {"speedup_vs_bruteforce": plain["brute_force"]["ms_per_step"] / batched_ms}
+    if "per_family_same_kernel" in plain:
+        out["speedup_vs_plain_same_kernel"] = (plain["per_family_same_kernel"]["ms_per_step"] /
+                                               batched_ms)
+    out["persistent_multi_family_vs_batched"] = (
+        plain["persistent_multi_family"]["ms_per_step"] / batched_ms)
+    return out
+
+
+def plain_forms(f, plan, pams, args, sp, timed, comps, steps=3):
+    """The same scan in the forms the batched one is compared with, each timed
+    with CUDA events and its hit keys kept (sorted) for a key-set comparison:
+    * brute_force: scan mode 0, one launch per PAM family and strand, every
+      guide compared per PAM-passing position (the plain drop-in);
+    * per_family_same_kernel: the autotuned index forms, one launch per PAM
+      family, launched one after another without a graph;
+    * persistent_multi_family: the prefiltered kernel over all families in one
+      persistent launch (warps claim chunks family by family), graph-captured.
+    The plan's autotuned tuning is restored afterwards."""
+    from beguidedoff_gb300 import _native
+
+    eng, st, K = f._engine, f._strands, args.max_mm
+    choice = f.last_choice
+    out = {}
+
+    def run(name, mode, step_fn, n_steps):
+        step_fn()
+        eng.complete(plan, st, [0, 3], K, mode, sp)   # the buffer then fits every hit
+        ms, tot = timed(step_fn, n_steps)
+        n, k = eng.collect(sp)
+        out[name] = {"mode": mode, "ms_per_step": tot / n_steps,
+                     "value": comps / (tot / n_steps / 1e3), "hits_per_step": n, "_k": k}
+
+    run("brute_force", 0, lambda: eng.launch(plan, st, [0, 3], K, 0, sp), max(1, steps - 1))
+    if choice is not None:
+        tune = tuple(choice.tuning) + (0,) * (9 - len(choice.tuning))
+        if not tune[3]:   # a single-launch form: the same form, one launch per family
+            plan.set_tuning(*(tune[:3] + (1,) + tune[4:]))
+        run("per_family_same_kernel", 2, lambda: eng.launch(plan, st, [0, 3], K, 2, sp), steps)
+        out["per_family_same_kernel"]["form"] = choice.name
+    plan.set_tuning(2048, 0, 0, 0, 0, 1, 0, 0, 1)
+    g = _native.Graph(eng, plan, st, [0, 3], K, 2)
+    try:
+        run("persistent_multi_family", 2, lambda: g.replay(sp), steps)
+    finally:
+        g.close()
+    if choice is not None:
+        choice.apply(plan, pams)
+    return out
+
+
 def bench_ours(args, ws, rank, local):
     import torch
 
@@ -512,6 +632,7 @@ def bench_ours(args, ws, rank, local):
     pams = guide_pams(args, len(guides))
     if dense:
         guides = dense_guides(genome["repeat_families"], pams)
+    guides = sacas9_extend(guides, pams)
     guides, pams = select_families(args, guides, pams)
     args.guides = len(guides)
     t0 = time.perf_counter()
@@ -559,15 +680,12 @@ def bench_ours(args, ws, rank, local):
         torch.cuda.synchronize()
         return [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)], ev[0].elapsed_time(ev[-1])
 
-    # the plain form (one kernel per PAM family and strand) for comparison
+    # the plain forms for comparison: the brute-force kernel (one launch per
+    # PAM family and strand, every guide compared) and the autotuned index
+    # forms launched one per family without a graph
     plain = None
     if args.config == "mixed" and args.mode != 0:
-        for _ in range(2):
-            eng.launch(plan, f._strands, [0, 3], args.max_mm, 0, sp)
-        ps, pt = timed(lambda: eng.launch(plan, f._strands, [0, 3], args.max_mm, 0, sp),
-                       max(2, args.steps // 2))
-        plain = {"mode": 0, "ms_per_step": pt / len(ps), "value": comps / (pt / len(ps) / 1e3),
-                 "hits_per_step": eng.hit_count(sp)}
+        plain = plain_forms(f, plan, pams, args, sp, timed, comps)
 
     # -------- device-resident kernel timing (value) --------
     graph = None
@@ -616,10 +734,17 @@ def bench_ours(args, ws, rank, local):
     t_max = dist_max(total_ms / 1e3, ws)
     hits = eng.hit_count(sp)
     pairs = eng.pairs_evaluated(sp)
+    # the timed form's hit keys, for the parity check and the plain forms
+    gpu_keys = None
+    if hits <= eng.info()["hit_capacity"]:
+        _, gpu_keys = eng.collect(sp)
     if graph is not None:
         graph.close()
     if plain is not None:
-        plain["hits_equal"] = plain["hits_per_step"] == hits
+        for form in plain.values():
+            k = form.pop("_k", None)
+            form["keys_equal"] = bool(gpu_keys is not None and k is not None and
+                                      np.array_equal(k, gpu_keys))
 
     # -------- roofline: the compare loop is POPC-bound (1 POPC per pair) --------
     popc_peak = _native.probe_int_throughput(1, local)
@@ -682,13 +807,32 @@ def bench_ours(args, ws, rank, local):
               "d2h_bytes_per_step": (x3["d2h"] - x2["d2h"]) // args.steps}
 
     # -------- CPU baseline (oracle, all host cores, bounded sample) --------
-    cpu = None
+    cpu, parity = None, None
     if rank == 0 and ws == 1 and not args.no_cpu:
         genome["_nm_fwd_le"], genome["_nm_rc_le"] = f._n_mask_fwd, f._n_mask_rc
         rate, threads, sample, dt = cpu_scan_rate(genome, guides, args.max_mm, args.cpu_seconds,
                                                   pams=pams)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": sample + f" ({dt:.1f} s, oracle/scan_oracle.c OpenMP)"}
+        # the timed scan's keys inside sampled ranges against the oracle
+        if gpu_keys is not None:
+            n_r, span = (8, 1_000_000) if dense else (16, 2_000_000)
+            parity = range_parity(
+                [(genome["genome_forward"], f._n_mask_fwd, 0), (genome["genome_rc"], f._n_mask_rc, 3)],
+                total, guides, pams, args.max_mm, gpu_keys,
+                sampled_ranges(lens, blocks, n_r, span))
+
+    # the batched mixed-PAM and serving records, on the resident genome
+    subs = None
+    if args.config == "plain" and ws == 1 and not args.no_subrecords:
+        subs = {}
+        t0 = time.perf_counter()
+        subs["mixed1000"] = sub_mixed(f, lens, blocks, args, sp, timed)
+        subs["mixed1000"]["seconds"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        subs["serve"] = serve_run(genome, total, local, 20.0, 6.0, 2, 16, 2048,
+                                  baselines=("same_kernel",))
+        subs["serve"]["seconds"] = time.perf_counter() - t0
 
     if rank == 0:
         value = replica_value(ws, comps, t_max / args.steps)
@@ -733,6 +877,8 @@ def bench_ours(args, ws, rank, local):
             "data": "synthetic", "config": workload_config(args, lens),
             "roofline": roof,
             "cpu_baseline": cpu,
+            "parity": parity,
+            "subrecords": subs,
             "e2e": {"value": ws * comps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "s_per_step": e2e_s,
                     "rows": len(table), "launches": e2e_launches // args.steps,
@@ -744,9 +890,8 @@ def bench_ours(args, ws, rank, local):
             "autotune": autotune,
             "epilogue": epi,
             "graph": graph is not None,
-            "plain_form": plain,
-            "speedup_vs_plain": (plain["ms_per_step"] / (1e3 * t_max / args.steps)
-                                 if plain else None),
+            "plain_forms": plain,
+            **(speedups(plain, 1e3 * t_max / args.steps) if plain else {}),
             "clocks": clk,
             "hits_per_step": hits,
             "step_ms": step_ms,
@@ -798,20 +943,17 @@ def _table_rows(t):
     return [dict(r) for r in t.rows()] if hasattr(t, "rows") else t.to_dict("records")
 
 
-def bench_serve(args, ws, rank, local):
-    """Serving loop: the same request trace through the continuous-batching
-    server and through serial per-request plain launches (scan mode 0, one
-    request at a time in arrival order, each waiting for the previous one)."""
-    from beguidedoff_gb300 import _native, build
+def serve_run(genome, total, local, rate, duration, slots, memory_gb, batch_guides,
+              baselines=("same_kernel", "brute_force")):
+    """A seeded request trace through the continuous-batching server, then
+    through serial per-request search() calls on the same trace: in the
+    server's own autotuned forms (same_kernel: the server's finder, one request
+    at a time) and, optionally, in the brute-force form (scan mode 0)."""
     from beguidedoff_gb300.finder import beguidedoff
     from beguidedoff_gb300.serving import SearchServer
 
-    build.build()
-    lens, blocks, _ = make_workload(args.genome_bp, 1)
-    total = int(lens.sum())
-    genome = _native.synth_genome(7, lens, blocks, thresholds=(76, 128, 180), device=local)
-    trace = serve_trace(args.rate, args.duration)
-    warm = serve_trace(args.rate, min(3.0, args.duration), seed=99)
+    trace = serve_trace(rate, duration)
+    warm = serve_trace(rate, min(3.0, duration), seed=99)
     n_guides = sum(len(g) for _, g, _ in trace)
     comps = n_guides * 2 * (total - 26)
 
@@ -843,9 +985,8 @@ def bench_serve(args, ws, rank, local):
             lat.append(time.perf_counter() - (t0 + t))
         return lat, time.perf_counter() - t0, res
 
-    clocks = ClockSampler(local).start()
-    srv = SearchServer(genome_data=genome, device=f"cuda:{local}", n_slots=args.slots,
-                       memory_bytes=args.serve_memory << 30, max_batch_guides=args.batch_guides)
+    srv = SearchServer(genome_data=genome, device=f"cuda:{local}", n_slots=slots,
+                       memory_bytes=memory_gb << 30, max_batch_guides=batch_guides)
     t_tune = time.perf_counter()
     srv.warmup()
     t_tune = time.perf_counter() - t_tune
@@ -861,49 +1002,142 @@ def bench_serve(args, ws, rank, local):
         "batches": len(batches),
         "requests_per_batch": float(np.mean([b["requests"] for b in batches])),
         "guides_per_batch": float(np.mean([b["guides"] for b in batches])),
-        "slots": args.slots, "memory_gb": args.serve_memory,
-        "max_batch_guides": args.batch_guides, "tuning_warmup_s": t_tune,
+        "slots": slots, "memory_gb": memory_gb,
+        "max_batch_guides": batch_guides, "tuning_warmup_s": t_tune,
         "batch_seconds": {k: float(np.mean([b.get(k, 0.0) for b in batches]))
                           for k in ("seconds", "plan_s", "scan_s", "epilogue_s", "assemble_s")},
         "autotune": {f"k{k[0]}/size{k[1]}": v.name for k, v in
                      (srv.finder._tuner.cache.items() if srv.finder._tuner else [])}})
+    serial = {}
+    same = True
+    # serial, one request at a time, in the server's own tuned forms
+    if "same_kernel" in baselines:
+        replay_serial(srv.finder, warm[:4])
+        lat_s, wall_s, res_s = replay_serial(srv.finder, trace)
+        serial["same_kernel"] = _latency_stats(lat_s, wall_s, n_guides, comps)
+        same = same and all(_table_rows(a) == _table_rows(b) for a, b in zip(res_b, res_s))
     srv.close()
-    base = beguidedoff(None, max_mismatches=4, genome_data=genome, device=f"cuda:{local}",
-                       scan_mode=0)
-    replay_serial(base, warm[:4])
-    lat_s, wall_s, res_s = replay_serial(base, trace)
-    base.close()
-    clk = clocks.stop()
-    ser_stats = _latency_stats(lat_s, wall_s, n_guides, comps)
-    same = all(_table_rows(a) == _table_rows(b) for a, b in zip(res_b, res_s))
+    if "brute_force" in baselines:
+        base = beguidedoff(None, max_mismatches=4, genome_data=genome, device=f"cuda:{local}",
+                           scan_mode=0)
+        replay_serial(base, warm[:4])
+        lat_s, wall_s, res_s = replay_serial(base, trace)
+        base.close()
+        serial["brute_force"] = _latency_stats(lat_s, wall_s, n_guides, comps)
+        same = same and all(_table_rows(a) == _table_rows(b) for a, b in zip(res_b, res_s))
     h2d = sum(b["h2d"] - a["h2d"] for a, b in zip(x0, x1))
     d2h = sum(b["d2h"] - a["d2h"] for a, b in zip(x0, x1))
+    out = {"requests": len(trace), "guides": n_guides, "rate_per_s": rate,
+           "duration_s": duration, "serving": srv_stats, "serial": serial,
+           "results_identical": same, "gpu_launches": launches,
+           "h2d_bytes_per_request": h2d // max(1, len(trace)),
+           "d2h_bytes_per_request": d2h // max(1, len(trace))}
+    for name, st in serial.items():
+        out[f"p50_speedup_vs_serial_{name}"] = st["p50_ms"] / srv_stats["p50_ms"]
+        out[f"p99_speedup_vs_serial_{name}"] = st["p99_ms"] / srv_stats["p99_ms"]
+    return out
+
+
+def bench_serve(args, ws, rank, local):
+    """Serving loop: the same request trace through the continuous-batching
+    server and through serial per-request search() calls (the server's own
+    tuned forms, and the brute-force form)."""
+    from beguidedoff_gb300 import _native, build
+
+    build.build()
+    lens, blocks, _ = make_workload(args.genome_bp, 1)
+    total = int(lens.sum())
+    genome = _native.synth_genome(7, lens, blocks, thresholds=(76, 128, 180), device=local)
+    clocks = ClockSampler(local).start()
+    r = serve_run(genome, total, local, args.rate, args.duration, args.slots, args.serve_memory,
+                  args.batch_guides)
+    clk = clocks.stop()
+    st = r["serving"]
     out = {
-        "metric": METRIC, "value": srv_stats["cmp_per_s"], "unit": UNIT, "n_gpus": ws,
-        "steps": len(trace), "warmup": len(warm), "ms_per_step": srv_stats["mean_ms"],
+        "metric": METRIC, "value": st["cmp_per_s"], "unit": UNIT, "n_gpus": ws,
+        "steps": r["requests"], "warmup": 0, "ms_per_step": st["mean_ms"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic",
         "config": {"workload": (f"serving loop: synthetic {total / 1e9:.2f} Gbp resident, Poisson "
                                 f"arrivals at {args.rate} req/s for {args.duration} s, 1-500 "
                                 f"guides per request (log-uniform), PAM families and editors as "
                                 f"the batched config, max_mismatches 3-5; a step = one request"),
-                   "genome_bp": total, "requests": len(trace), "guides": n_guides,
+                   "genome_bp": total, "requests": r["requests"], "guides": r["guides"],
                    "rate_per_s": args.rate, "duration_s": args.duration,
                    "l2": "inputs larger than L2 (bit planes of both strands ~2.3 GB)"},
-        "serving": srv_stats, "serial_plain": ser_stats,
-        "p50_speedup": ser_stats["p50_ms"] / srv_stats["p50_ms"],
-        "p99_speedup": ser_stats["p99_ms"] / srv_stats["p99_ms"],
-        "results_identical": same,
-        "e2e": {"value": srv_stats["cmp_per_s"], "unit": UNIT,
-                "h2d_bytes_per_step": h2d // max(1, len(trace)),
-                "d2h_bytes_per_step": d2h // max(1, len(trace)),
+        **{k: v for k, v in r.items() if k not in ("requests", "guides")},
+        "e2e": {"value": st["cmp_per_s"], "unit": UNIT,
+                "h2d_bytes_per_step": r["h2d_bytes_per_request"],
+                "d2h_bytes_per_step": r["d2h_bytes_per_request"],
                 "note": "the genome stays resident; per request: guides, plan and epilogue "
                         "inputs up, epilogue results down"},
-        "gpu_launches": launches,
         "clocks": clk,
     }
     if rank == 0:
         print(json.dumps(out))
+
+
+def sub_mixed(f, lens, blocks, args, sp, timed, n_guides=1000, max_mm=5, steps=3):
+    """The batched mixed-PAM record on the genome already resident: 1,000
+    guides (NGG 40% NG 20% NNGRRT 15% NNNRRT 15% NRN 10%; the SaCas9 families
+    21 nt), max_mismatches 5; the autotuned batched form (one graph replay)
+    against the plain forms of plain_forms(), with key sets compared and the
+    keys checked against the oracle on sampled ranges."""
+    from types import SimpleNamespace
+
+    from beguidedoff_gb300 import _native
+
+    total = int(np.asarray(lens).sum())
+    rng = np.random.default_rng(12)
+    guides = ["".join(rng.choice(list("ACGT"), 20)) for _ in range(n_guides)]
+    pams = []
+    for pam, frac in MIXED_FAMILIES:
+        pams += [pam] * int(round(frac * n_guides))
+    pams = (pams + ["NGG"] * n_guides)[:n_guides]
+    guides = sacas9_extend(guides, pams)
+    comps = n_guides * 2 * (total - 26)
+    eng, st = f._engine, f._strands
+    plan = f._plan(guides, pams)
+    try:
+        t0 = time.perf_counter()
+        mode = f._mode_for(plan, pams, max_mm)
+        tune_s = time.perf_counter() - t0
+        choice = f.last_choice
+        forms = plain_forms(f, plan, pams, SimpleNamespace(max_mm=max_mm), sp, timed, comps,
+                            steps)
+        if mode in (2, 3):
+            g = _native.Graph(eng, plan, st, [0, 3], max_mm, mode)
+            step = lambda: g.replay(sp)  # noqa: E731
+        else:
+            g = None
+            step = lambda: eng.launch(plan, st, [0, 3], max_mm, mode, sp)  # noqa: E731
+        step()
+        eng.complete(plan, st, [0, 3], max_mm, mode, sp)
+        _, tot = timed(step, steps)
+        n, keys = eng.collect(sp)
+        if g is not None:
+            g.close()
+        batched_ms = tot / steps
+        for form in forms.values():
+            k = form.pop("_k", None)
+            form["keys_equal"] = bool(k is not None and keys is not None and
+                                      np.array_equal(k, keys))
+        out = {"workload": (f"batched mixed-PAM scan on the resident {total / 1e9:.2f} Gbp "
+                            f"genome: {n_guides} guides (NGG 40% NG 20% NNGRRT 15% NNNRRT 15% "
+                            f"NRN 10%, SaCas9 guides 21 nt), max_mismatches {max_mm}, both strands"),
+               "guides": n_guides, "max_mismatches": max_mm,
+               "batched": {"form": choice.name if choice else str(mode), "graph": g is not None,
+                           "ms_per_step": batched_ms, "value": comps / (batched_ms / 1e3),
+                           "hits_per_step": n},
+               "autotune_s": tune_s, "autotune": choice.as_dict() if choice else None,
+               "plain_forms": forms, **speedups(forms, batched_ms)}
+        if not args.no_cpu and keys is not None:
+            out["parity"] = range_parity(
+                [(f._strand_arrays[0], f._n_mask_fwd, 0), (f._strand_arrays[1], f._n_mask_rc, 3)],
+                total, guides, pams, max_mm, keys, sampled_ranges(lens, blocks, 4, 1_000_000))
+        return out
+    finally:
+        plan.close()
 
 
 def main():
@@ -932,6 +1166,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-subrecords", action="store_true",
+                    help="plain config: skip the mixed-PAM 1,000-guide and serving records")
     ap.add_argument("--families", default="", help="mixed/dense: keep only these PAM families "
                                                    "(comma list), e.g. NRN")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: requests per second")

@@ -18,7 +18,7 @@ TABLE_COLS = [
     "score", "n_offtargets_below_threshold",
 ]
 FINDER_CASES = ["planted_ngg", "mixed_pam", "n_gate", "n_gate_nomask", "overflow",
-                "overflow_capped", "repeats", "many_guides"]
+                "overflow_capped", "repeats", "many_guides", "sacas9_21nt"]
 
 
 @dataclass(frozen=True)

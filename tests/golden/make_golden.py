@@ -517,6 +517,33 @@ def case_convert():
     print("convert: ok")
 
 
+def case_sacas9_21nt():
+    """21-nt guides of the SaCas9 families (NNGRRT, NNNRRT) beside 20-nt NGG
+    guides.  The reference packs a 21-nt guide into 42 bits but compares only
+    its first 20 bases (40-bit mask) and tests the PAM right after them
+    (beguidedoff/encoding.py:70-75, cuda_search.py:239-275); sites are planted
+    both as the first 20 bases + PAM and as all 21 bases + PAM."""
+    rng = np.random.default_rng(2121)
+    chroms = {"chr1": rand_seq(rng, 30_000), "chr2": rand_seq(rng, 20_000)}
+    chroms = {k: add_n_runs(rng, v, 0.01, 50, 300) for k, v in chroms.items()}
+    specs = [(21, "NNGRRT"), (21, "NNNRRT"), (21, "NNGRRT"), (20, "NGG"), (21, "NGG")]
+    guides_seq = [rand_seq(rng, n) for n, _ in specs]
+    names = list(chroms)
+    for g, (n, pam) in zip(guides_seq, specs):
+        for k in range(8):
+            c = names[int(rng.integers(0, 2))]
+            core = g[:20] if k % 2 == 0 else g
+            chroms[c] = plant(rng, chroms[c], core, pam, int(rng.integers(0, 4)),
+                              "+" if rng.random() < 0.5 else "-")
+    guides = []
+    for i, (g, (n, pam)) in enumerate(zip(guides_seq, specs)):
+        et = ("ABE", "CBE", "CGE")[i % 3]
+        guides.append(GuideInput(f"sa_{i}", g, pam, "3prime", 3, 9, et))
+    runs = [{"kwargs": {"return_all": True, "count_score_threshold": 5.0}},
+            {"kwargs": {"return_all": False}}]
+    run_case("sacas9_21nt", chroms, guides, runs, max_mm=4, n_top=3)
+
+
 def case_config1():
     """The plain CPU-runnable configuration at its stated size (10 Mbp, 2
     chromosomes, 1% N in runs of 100-5,000 bp, 10 NGG guides x 20 planted
@@ -577,6 +604,7 @@ CASES = {
     "seam_5prime": case_seam_5prime,
     "convert": case_convert,
     "config1": case_config1,
+    "sacas9_21nt": case_sacas9_21nt,
 }
 
 if __name__ == "__main__":
