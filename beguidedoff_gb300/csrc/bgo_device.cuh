@@ -35,19 +35,20 @@ __device__ __forceinline__ uint32_t pam_test(uint32_t h, uint32_t l, uint32_t co
     return ~(((h ^ hv) & hc) | ((l ^ lv) & lc));
 }
 
-// Marks the granule of a key that did not fit the hit buffer.
-__device__ __forceinline__ void mark_dropped(uint64_t key, uint32_t *drop_bits, int64_t base1) {
+// Marks the granule (4,096 positions of one strand) of a key that did not fit
+// the hit buffer.
+__device__ __forceinline__ void mark_dropped(uint64_t pos, uint64_t slot, uint32_t *drop_bits,
+                                             int64_t base1) {
     if (!drop_bits) return;
-    const int64_t pos = (int64_t)((key >> 6) & 0xFFFFFFFFull);
-    const int64_t g = (((key >> 38) & 1ull) ? base1 : 0) + pos / 4096;
+    const int64_t g = (slot ? base1 : 0) + (int64_t)(pos / 4096);
     atomicOr(drop_bits + (g >> 5), 1u << (g & 31));
 }
 
 // Appends `key`; the lanes executing this call together share one atomicAdd.
-// A key past the buffer's capacity is counted and its granule marked.
-__device__ __forceinline__ void semit(uint64_t key, uint64_t *keys, int64_t cap,
-                                      unsigned long long *counter, uint32_t *drop_bits,
-                                      int64_t drop_base1) {
+// Returns true when the key did not fit (it is counted; the caller marks its
+// granule, so that this path stays small).
+__device__ __forceinline__ bool semit(uint64_t key, uint64_t *keys, int64_t cap,
+                                      unsigned long long *counter) {
     unsigned act = __activemask();
     int lane = threadIdx.x & 31;
     int leader = __ffs(act) - 1;
@@ -55,8 +56,11 @@ __device__ __forceinline__ void semit(uint64_t key, uint64_t *keys, int64_t cap,
     if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(act));
     base = __shfl_sync(act, base, leader);
     unsigned long long slot = base + (unsigned long long)__popc(act & ((1u << lane) - 1u));
-    if (slot < (unsigned long long)cap) keys[slot] = key;
-    else mark_dropped(key, drop_bits, drop_base1);
+    if (slot < (unsigned long long)cap) {
+        keys[slot] = key;
+        return false;
+    }
+    return true;
 }
 
 }  // namespace bgo

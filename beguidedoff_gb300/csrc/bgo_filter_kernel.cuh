@@ -147,16 +147,17 @@ __device__ __forceinline__ uint32_t at_least_two(const uint32_t (&x)[S]) {
     }
 }
 
-// The survivor rounds' view of a family's index, held in registers: region
-// j's descriptors start at seg_off[j] and its entries at seg_ent[j]; in the
-// shared-memory form also the descriptor, entry-index and guide-plane arrays.
-template <int K>
+// The survivor rounds' view of a family's index, held in registers and kept
+// small (the filter rounds around it are register-bound).  Shared form: per
+// region seg[j] = descriptor start | entry start << 16 (both < 2^16), and
+// sizes = descriptors | guide-plane byte offset << 15 of the family's block
+// at sidx.  Global form: descriptor starts seg[j] and entry starts ent[j].
+template <int K, int ISM>
 struct FiltView {
-    uint32_t seg_off[SegT<K, 1>::S], seg_ent[SegT<K, 1>::S];
+    uint32_t seg[SegT<K, 1>::S];
+    uint32_t ent[ISM ? 1 : SegT<K, 1>::S];
+    uint32_t sizes;
     uint32_t gbeg;  // first row of the family in the family-sorted guide table
-    const uint16_t *off16;
-    const uint16_t *idx16;
-    const uint2 *gpl;
 };
 
 // Survivor record: x = h20 | strand index << 31, y = l20, z = N bits of the
@@ -164,7 +165,7 @@ struct FiltView {
 // The full segment-index check of one survivor per lane (`valid` lanes): per
 // region the bucket of the key's single-substitution neighbourhood, then
 // every entry's full compare and the N correction (finish_candidate, as in
-// scan_seed_kernel).  The index is read from shared memory (ISM: fv holds the
+// scan_seed_kernel).  The index is read from shared memory (ISM: at sidx the
 // family's 16-bit descriptors, entry start | count << 12, then the
 // family-local guide index of each entry, then the family's guide planes) or
 // from global memory (32-bit descriptors, entry start | count << 16, entries
@@ -172,7 +173,9 @@ struct FiltView {
 // compared.
 template <int K, int ISM>
 __device__ __forceinline__ uint32_t filter_heavy(const ScanParams &p, const FilterArgs &fa,
-                                                 const FiltView<K> &fv, uint4 r, bool valid) {
+                                                 const unsigned char *sidx,
+                                                 const FiltView<K, ISM> &fv, uint4 r,
+                                                 bool valid) {
     using G = SegT<K, 1>;
     constexpr int S = G::S;
     const uint32_t h20 = r.x & 0xFFFFFu, l20 = r.y;
@@ -180,9 +183,9 @@ __device__ __forceinline__ uint32_t filter_heavy(const ScanParams &p, const Filt
     const uint32_t ne = (uint32_t)(si ? p.strand[1].n_encoded : p.strand[0].n_encoded);
     const uint64_t slot = (uint64_t)(si ? p.strand[1].slot : p.strand[0].slot);
     const uint64_t pos = (uint64_t)r.w;
-    const uint16_t *off16 = fv.off16;
-    const uint16_t *idx16 = fv.idx16;
-    const uint2 *gpl = fv.gpl;
+    const uint16_t *off16 = reinterpret_cast<const uint16_t *>(sidx);
+    const uint16_t *idx16 = off16 + (fv.sizes & 0x7FFFu);
+    const uint2 *gpl = reinterpret_cast<const uint2 *>(sidx + (fv.sizes >> 15));
     uint32_t cand = 0;
 #pragma unroll
     for (int j = 0; j < S; ++j) {
@@ -191,13 +194,13 @@ __device__ __forceinline__ uint32_t filter_heavy(const ScanParams &p, const Filt
         const uint32_t code = (((h20 >> st) & km) << kl) | ((l20 >> st) & km);
         uint32_t nn, e0;
         if (ISM) {
-            const uint32_t d = valid ? off16[fv.seg_off[j] + code] : 0u;
+            const uint32_t d = valid ? off16[(fv.seg[j] & 0xFFFFu) + code] : 0u;
             nn = d >> 12;
-            e0 = fv.seg_ent[j] + (d & 0xFFFu);
+            e0 = (fv.seg[j] >> 16) + (d & 0xFFFu);
         } else {
-            const uint32_t d = valid ? __ldg(fa.offsets + fv.seg_off[j] + code) : 0u;
+            const uint32_t d = valid ? __ldg(fa.offsets + fv.seg[j] + code) : 0u;
             nn = d >> 16;
-            e0 = fv.seg_ent[j] + (d & 0xFFFFu);
+            e0 = fv.ent[ISM ? 0 : j] + (d & 0xFFFFu);
         }
         cand += nn;
         for (uint32_t i = 0; i < nn; ++i) {
@@ -213,7 +216,8 @@ __device__ __forceinline__ uint32_t filter_heavy(const ScanParams &p, const Filt
             const int cm = __popc(m);
             if (cm <= K) {
                 if (!ISM) gi = __ldg(fa.entry_idx + e0 + i);
-                finish_candidate<K, 1>(p, m, cm, e, gi, j, r.z, ne, slot, pos, fv.gbeg);
+                if (finish_candidate<K, 1>(p, m, cm, e, gi, j, r.z, ne, slot, pos, fv.gbeg))
+                    mark_dropped(pos, slot, p.drop_bits, p.drop_base1);
             }
         }
     }
@@ -256,7 +260,14 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
     // rescan scans only the chunks of its list (items index the list)
     const int chunks0 = (int)p.strand[0].n_tiles;
     const int n_chunks = p.chunk_list ? (int)p.n_list : (int)p.tiles_total;
-    auto chunk_at = [&](int i) -> int { return p.chunk_list ? (int)p.chunk_list[i] : i; };
+    // the list pointer is read from shared memory where it is used (once per
+    // chunk), so that the rounds keep no register for it
+    __shared__ const uint32_t *sChunkList;
+    if (t == 0) sChunkList = p.chunk_list;
+    auto chunk_at = [&](int i) -> int {
+        const uint32_t *cl = *(const uint32_t *volatile *)&sChunkList;
+        return cl ? (int)cl[i] : i;
+    };
     // Copies chunk c's words [c*CH/32, c*CH/32 + kWords) of the three planes
     // into buffer b (the planes are padded so that the copy never leaves them,
     // and zero beyond total_bp).  One lane issues the three bulk copies.
@@ -339,21 +350,23 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
         const uint32_t win_off = F.three_prime ? 0u : (uint32_t)F.plen;
         const int n_tests = sSF->n_tests;
         const bool all_fixed = sSF->pam_generic == 0;
-        FiltView<K> fv;
+        FiltView<K, ISM> fv;
         fv.gbeg = (uint32_t)F.gbeg;
+        fv.sizes = 0;
         if (ISM) {
+            // descriptors < 2^15 (<= 4 regions of 4,096 keys), guide planes
+            // at a byte offset < 2^17 (the host keeps the block in 227 KB)
             const uint2 sz = fa.fam_sizes[fi];
-            fv.off16 = reinterpret_cast<const uint16_t *>(sIdxBlk);
-            fv.idx16 = fv.off16 + sz.x;
-            fv.gpl = reinterpret_cast<const uint2 *>(sIdxBlk + ((sz.x * 2u + sz.y * 2u + 15u) & ~15u));
-        } else {
-            fv.off16 = fv.idx16 = nullptr;
-            fv.gpl = nullptr;
+            fv.sizes = sz.x | (((sz.x * 2u + sz.y * 2u + 15u) & ~15u) << 15);
         }
 #pragma unroll
         for (int j = 0; j < S; ++j) {
-            fv.seg_off[j] = ISM ? sSF->seg[j].off - sSF->seg[0].off : sSF->seg[j].off;
-            fv.seg_ent[j] = (ISM ? 0u : sSF->list_off) + sSF->seg[j].ent;
+            if (ISM) {
+                fv.seg[j] = (sSF->seg[j].off - sSF->seg[0].off) | (sSF->seg[j].ent << 16);
+            } else {
+                fv.seg[j] = sSF->seg[j].off;
+                fv.ent[ISM ? 0 : j] = sSF->list_off + sSF->seg[j].ent;
+            }
         }
         int qn = 0;  // survivors queued (warp-uniform)
 
@@ -557,7 +570,8 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                             qn += __popc(bal);
                             if (qn >= 32) {
                                 __syncwarp();
-                                cand += filter_heavy<K, ISM>(p, fa, fv, wQ[qn - 32 + lane], true);
+                                cand += filter_heavy<K, ISM>(p, fa, sIdxBlk, fv, wQ[qn - 32 + lane],
+                                                             true);
                                 qn -= 32;
                                 __syncwarp();
                             }
@@ -574,7 +588,7 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
         if (qn > 0) {
             __syncwarp();
             const bool v = lane < qn;
-            cand += filter_heavy<K, ISM>(p, fa, fv, wQ[v ? lane : 0], v);
+            cand += filter_heavy<K, ISM>(p, fa, sIdxBlk, fv, wQ[v ? lane : 0], v);
             __syncwarp();
         }
     }

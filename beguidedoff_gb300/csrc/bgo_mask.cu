@@ -65,8 +65,9 @@ __device__ __forceinline__ void mask_finish(const ScanParams &p, int cm, uint2 e
     }
     if (mmf > K) return;
     const uint32_t row = __ldg(&p.guides[row_at].row);
-    semit(((uint64_t)row << 39) | (slot << 38) | (pos << 6) | (uint64_t)mmf, p.keys, p.cap,
-          p.counter, p.drop_bits, p.drop_base1);
+    if (semit(((uint64_t)row << 39) | (slot << 38) | (pos << 6) | (uint64_t)mmf, p.keys, p.cap,
+          p.counter))
+        mark_dropped(pos, slot, p.drop_bits, p.drop_base1);
 }
 
 template <int CH>

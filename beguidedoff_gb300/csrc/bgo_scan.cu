@@ -63,7 +63,7 @@ __device__ __forceinline__ void emit_key(uint64_t key, uint64_t *keys, int64_t c
     base = __shfl_sync(act, base, leader);
     unsigned long long slot = base + (unsigned long long)__popc(act & ((1u << lane) - 1u));
     if (slot < (unsigned long long)cap) keys[slot] = key;
-    else mark_dropped(key, drop_bits, drop_base1);
+    else mark_dropped((key >> 6) & 0xFFFFFFFFull, (key >> 38) & 1ull, drop_bits, drop_base1);
 }
 
 __global__ void __launch_bounds__(kTileThreads) scan_kernel(ScanParams p) {

@@ -58,9 +58,10 @@ struct SegT {
 
 // The full check of a candidate whose raw count cm <= K, found through
 // region j: emits the hit if j is its first region with <= TOL mismatches
-// and it stays within K after the N correction.
+// and it stays within K after the N correction.  Returns true when the hit
+// did not fit the hit buffer (the caller marks its granule).
 template <int K, int TOL>
-__device__ __noinline__ void finish_candidate(const ScanParams &p, uint32_t m, int cm, uint2 e,
+__device__ __noinline__ bool finish_candidate(const ScanParams &p, uint32_t m, int cm, uint2 e,
                                               uint32_t idx, int j, uint32_t n20g, uint32_t ne,
                                               uint64_t slot, uint64_t pos, uint32_t gbeg) {
     using G = SegT<K, TOL>;
@@ -69,17 +70,17 @@ __device__ __noinline__ void finish_candidate(const ScanParams &p, uint32_t m, i
     for (int jj = 0; jj < G::S - 1; ++jj)
         if (jj < j)
             first = first && __popc((m >> G::start(jj)) & ((1u << G::klen(jj)) - 1u)) > TOL;
-    if (!first) return;
+    if (!first) return false;
     int mmf = cm;
     if (n20g) {
         const uint32_t eh = (ne & 2u) ? e.x : ~e.x;
         const uint32_t el = (ne & 1u) ? e.y : ~e.y;
         mmf = cm + __popc(n20g & eh & el);
     }
-    if (mmf > K) return;
+    if (mmf > K) return false;
     const uint32_t row = __ldg(&p.guides[gbeg + idx].row);
-    semit(((uint64_t)row << 39) | (slot << 38) | (pos << 6) | (uint64_t)mmf, p.keys, p.cap,
-          p.counter, p.drop_bits, p.drop_base1);
+    return semit(((uint64_t)row << 39) | (slot << 38) | (pos << 6) | (uint64_t)mmf, p.keys, p.cap,
+                 p.counter);
 }
 
 // CTA shapes by MINB: 3 or 4 CTAs of 256 threads per SM; or one CTA per SM
@@ -328,8 +329,9 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, SeedCta<MINB>::kPerSm
                                     const uint32_t ei = e0v[j] + a;
                                     const uint2 e = sEnt[ei];
                                     const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
-                                    finish_candidate<K, TOL>(p, m, __popc(m), e, sIdx[ei], j, n20g,
-                                                             ne, slot, pos, gbeg);
+                                    if (finish_candidate<K, TOL>(p, m, __popc(m), e, sIdx[ei], j, n20g,
+                                                             ne, slot, pos, gbeg))
+                                    mark_dropped(pos, slot, p.drop_bits, p.drop_base1);
                                 }
                             }
                         }
@@ -347,8 +349,9 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, SeedCta<MINB>::kPerSm
                                 const uint32_t m = (h20 ^ e.x) | (l20 ^ e.y);
                                 const int cm = __popc(m);
                                 if (cm <= K)
-                                    finish_candidate<K, TOL>(p, m, cm, e, sIdx[ei], j, n20g,
-                                                             ne, slot, pos, gbeg);
+                                    if (finish_candidate<K, TOL>(p, m, cm, e, sIdx[ei], j, n20g,
+                                                             ne, slot, pos, gbeg))
+                                    mark_dropped(pos, slot, p.drop_bits, p.drop_base1);
                             }
                         }
                         continue;
@@ -386,9 +389,10 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, SeedCta<MINB>::kPerSm
                             const uint32_t m = (r.x ^ e.x) | (r.y ^ e.y);
                             const int cm = __popc(m);
                             if (cm <= K)
-                                finish_candidate<K, TOL>(p, m, cm, e, sIdx[e0 + i], j, r.z,
+                                if (finish_candidate<K, TOL>(p, m, cm, e, sIdx[e0 + i], j, r.z,
                                                          ne, slot, (uint64_t)(base + r.w),
-                                                         gbeg);
+                                                         gbeg))
+                                    mark_dropped((uint64_t)(base + r.w), slot, p.drop_bits, p.drop_base1);
                         }
                     }
                     __syncwarp();
