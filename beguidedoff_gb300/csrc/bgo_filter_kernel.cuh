@@ -231,10 +231,12 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
     using G = SegT<K, 1>;
     constexpr int S = G::S;
     using C = FiltChunk<CH>;
-    extern __shared__ __align__(128) unsigned char smem[];
-    uint8_t *sTab = smem;
-    SeedFam *sSF = reinterpret_cast<SeedFam *>(smem + FT::kBytesAl);
-    unsigned char *sIdxBlk = smem + FT::kBytesAl + (sizeof(SeedFam) + 15) / 16 * 16;
+    // (its own name: the segment-index kernels in the same translation unit
+    // declare the dynamic block with 16-byte alignment)
+    extern __shared__ __align__(128) unsigned char filt_smem[];
+    uint8_t *sTab = filt_smem;
+    SeedFam *sSF = reinterpret_cast<SeedFam *>(filt_smem + FT::kBytesAl);
+    unsigned char *sIdxBlk = filt_smem + FT::kBytesAl + (sizeof(SeedFam) + 15) / 16 * 16;
     unsigned char *slices = sIdxBlk + (ISM ? fa.idx_smem_bytes : 0);
     __shared__ unsigned long long sCand;
 
