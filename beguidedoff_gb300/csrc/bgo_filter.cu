@@ -29,8 +29,10 @@
 // warp, every lane runs the segment index on one survivor: per region the
 // bucket of the key's single-substitution neighbourhood, then the reference's
 // full compare and N correction (finish_candidate, as in scan_seed_kernel).
-// Each lane tests two list positions per round, and a lane without a survivor
-// stores into a spare queue slot, so the round has no per-lane branch.
+// Each lane tests three list positions per round; the round's survivors go
+// into the queue together (a lane without a survivor stores into a spare
+// slot, so the round has no per-lane branch), and the queue is drained a warp
+// at a time.
 //
 // Survivor index.  When the largest launch family's index fits beside the
 // tables and slices, and its descriptors fit 16 bits (entry starts < 4,096,
@@ -60,6 +62,8 @@
 #include "bgo_filter_kernel.cuh"
 
 namespace bgo {
+
+size_t filter_smem_limit() { return (size_t)kFilterSmemLimit; }
 
 uint32_t filter_tab_bytes(int K) {
     switch (K) {

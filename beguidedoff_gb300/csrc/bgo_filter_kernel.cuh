@@ -20,7 +20,6 @@ namespace bgo {
 #endif
 constexpr int kFilterThreads = BGO_FILTER_THREADS;  // one CTA per SM
 constexpr int kFilterWarps = kFilterThreads / 32;
-constexpr int kSurvCap = 64;         // per-warp survivor queue (two rounds)
 constexpr int kClaimChunks = 2;      // chunks per work claim
 #ifndef BGO_FILTER_STATIC_QUARTERS
 #define BGO_FILTER_STATIC_QUARTERS 3
@@ -28,14 +27,21 @@ constexpr int kClaimChunks = 2;      // chunks per work claim
 // quarters of a family's chunks handed out in a static grid stride
 constexpr int kStaticQuarters = BGO_FILTER_STATIC_QUARTERS;
 #ifndef BGO_FILTER_PER
-#define BGO_FILTER_PER 2
+#define BGO_FILTER_PER 3
 #endif
 // list positions per lane in one filter round
 constexpr int kFilterPer = BGO_FILTER_PER;
+// per-warp survivor queue: up to 31 left from earlier rounds plus one
+// round's 32 * kFilterPer
+constexpr int kSurvCap = 32 * (kFilterPer + 1);
 // a bounded wait on a chunk copy gives up after this many nanoseconds
 constexpr unsigned long long kCopyWaitNs = 2000000000ull;
+// static shared memory of the kernel (counters, the chunk-order start and
+// the warps' index views) stays below this; the dynamic block takes the rest
+// of the 227 KB a CTA may hold
+constexpr int kFilterStaticSmem = 1024;
 // dynamic shared memory a prefiltered form may take
-constexpr int kFilterSmemLimit = 227 * 1024;
+constexpr int kFilterSmemLimit = 227 * 1024 - kFilterStaticSmem;
 
 // Filter regions: the tolerance-1 regions SegT<K, 1> of the segment index,
 // keyed by their first <= kFilterKeyLen bases; region j's table of one byte
@@ -239,6 +245,8 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
     unsigned char *sIdxBlk = filt_smem + FT::kBytesAl + (sizeof(SeedFam) + 15) / 16 * 16;
     unsigned char *slices = sIdxBlk + (ISM ? fa.idx_smem_bytes : 0);
     __shared__ unsigned long long sCand;
+    __shared__ FiltView<K, ISM> sFV[kFilterWarps];
+    static_assert(sizeof(sFV) + 64 <= kFilterStaticSmem, "static shared memory within its reserve");
 
     const int t = threadIdx.x;
     const int lane = t & 31;
@@ -292,19 +300,32 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
     // Chunk order of a warp: the first kStaticQuarters/4 of the chunks in a
     // static grid stride over all warps (no atomics), the rest claimed in runs
     // of kClaimChunks from the family's counter, so that warps that finish
-    // early take the tail.
-    const int n_warps = (int)gridDim.x * kFilterWarps;
-    const int gwarp = (int)blockIdx.x * kFilterWarps + warp;
-    const int static_rounds = (int)((int64_t)n_chunks * kStaticQuarters / 4 / n_warps);
-    const int dyn0 = static_rounds * n_warps;
-    int round = 0, run = 0, run_end = 0;
+    // early take the tail.  A warp's place in it is three registers: the next
+    // chunk, the end of the current stretch and the stride (all warps in the
+    // static part, 1 in a claimed run); where the claimed chunks start is in
+    // shared memory.
+    __shared__ int sDyn0;
+    if (t == 0) {
+        const int n_warps = (int)gridDim.x * kFilterWarps;
+        sDyn0 = (int)((int64_t)n_chunks * kStaticQuarters / 4 / n_warps) * n_warps;
+    }
+    int run = 0, run_end = 0, step = 0;
+    auto start_order = [&]() {
+        run = (int)blockIdx.x * kFilterWarps + warp;
+        run_end = *(volatile int *)&sDyn0;
+        step = (int)gridDim.x * kFilterWarps;
+    };
     auto next_chunk = [&](int fi) -> int {
-        if (round < static_rounds) return gwarp + (round++) * n_warps;
-        if (run < run_end) return run++;
+        if (run < run_end) {
+            const int c = run;
+            run += step;
+            return c;
+        }
         uint32_t c = 0;
         if (lane == 0) c = atomicAdd(fa.work + fi, (uint32_t)kClaimChunks);
-        run = dyn0 + (int)__shfl_sync(0xFFFFFFFFu, c, 0);
+        run = *(volatile int *)&sDyn0 + (int)__shfl_sync(0xFFFFFFFFu, c, 0);
         run_end = run + kClaimChunks < n_chunks ? run + kClaimChunks : n_chunks;
+        step = 1;
         return run < n_chunks ? run++ : n_chunks;
     };
 
@@ -352,27 +373,32 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
         const uint32_t win_off = F.three_prime ? 0u : (uint32_t)F.plen;
         const int n_tests = sSF->n_tests;
         const bool all_fixed = sSF->pam_generic == 0;
-        FiltView<K, ISM> fv;
-        fv.gbeg = (uint32_t)F.gbeg;
-        fv.sizes = 0;
-        if (ISM) {
-            // descriptors < 2^15 (<= 4 regions of 4,096 keys), guide planes
-            // at a byte offset < 2^17 (the host keeps the block in 227 KB)
-            const uint2 sz = fa.fam_sizes[fi];
-            fv.sizes = sz.x | (((sz.x * 2u + sz.y * 2u + 15u) & ~15u) << 15);
-        }
-#pragma unroll
-        for (int j = 0; j < S; ++j) {
+        // the warp's view of the family's survivor index: written by lane 0,
+        // read by the survivor checks (kept out of the rounds' registers)
+        FiltView<K, ISM> &fv = sFV[warp];
+        if (lane == 0) {
+            fv.gbeg = (uint32_t)F.gbeg;
+            fv.sizes = 0;
             if (ISM) {
-                fv.seg[j] = (sSF->seg[j].off - sSF->seg[0].off) | (sSF->seg[j].ent << 16);
-            } else {
-                fv.seg[j] = sSF->seg[j].off;
-                fv.ent[ISM ? 0 : j] = sSF->list_off + sSF->seg[j].ent;
+                // descriptors < 2^15 (<= 4 regions of 4,096 keys), guide
+                // planes at a byte offset < 2^17 (the block stays in 227 KB)
+                const uint2 sz = fa.fam_sizes[fi];
+                fv.sizes = sz.x | (((sz.x * 2u + sz.y * 2u + 15u) & ~15u) << 15);
+            }
+#pragma unroll
+            for (int j = 0; j < S; ++j) {
+                if (ISM) {
+                    fv.seg[j] = (sSF->seg[j].off - sSF->seg[0].off) | (sSF->seg[j].ent << 16);
+                } else {
+                    fv.seg[j] = sSF->seg[j].off;
+                    fv.ent[ISM ? 0 : j] = sSF->list_off + sSF->seg[j].ent;
+                }
             }
         }
+        __syncwarp();
         int qn = 0;  // survivors queued (warp-uniform)
 
-        round = run = run_end = 0;
+        start_order();
         int cur = next_chunk(fi);
         int buf = 0;
         if (cur < n_chunks) issue(chunk_at(cur), buf);
@@ -455,6 +481,9 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
             int total = 0, off0 = 0, cnt = 0;
 #pragma unroll 1
             for (int pass_i = 0; pass_i < C::kPasses; ++pass_i) {
+                // a further pass only while listed positions remain (the
+                // tests are not run again to find that the chunk is done)
+                if (pass_i > 0 && pass_i * C::kListCap >= total) break;
                 uint32_t pass[C::kRows];
                 pam_pass(pass);
                 if (pass_i == 0) {
@@ -551,10 +580,17 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                         lv[v] = l20;
                         keep[v] = has && kp;
                     }
+                    // the round's survivors into the queue at once, then a
+                    // warp of them through the index while the queue holds one
+                    uint32_t bal[kFilterPer], any_bal = 0;
 #pragma unroll
                     for (int v = 0; v < kFilterPer; ++v) {
-                        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep[v]);
-                        if (bal) {
+                        bal[v] = __ballot_sync(0xFFFFFFFFu, keep[v]);
+                        any_bal |= bal[v];
+                    }
+                    if (any_bal) {
+#pragma unroll
+                        for (int v = 0; v < kFilterPer; ++v) {
                             const uint32_t s = sv[v];
                             uint32_t n20g = 0;
                             if (has_n) {
@@ -566,17 +602,17 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                                 n20g = n26 ? n20 : 0u;
                             }
                             // a lane without a survivor stores into the spare slot
-                            const int at = keep[v] ? qn + __popc(bal & lt_mask) : kSurvCap;
+                            const int at = keep[v] ? qn + __popc(bal[v] & lt_mask) : kSurvCap;
                             wQ[at] = make_uint4((hv[v] & 0xFFFFFu) | strand_bit, lv[v] & 0xFFFFFu,
                                                 n20g, base32 + s);
-                            qn += __popc(bal);
-                            if (qn >= 32) {
-                                __syncwarp();
-                                cand += filter_heavy<K, ISM>(p, fa, sIdxBlk, fv, wQ[qn - 32 + lane],
-                                                             true);
-                                qn -= 32;
-                                __syncwarp();
-                            }
+                            qn += __popc(bal[v]);
+                        }
+                        while (qn >= 32) {
+                            __syncwarp();
+                            cand += filter_heavy<K, ISM>(p, fa, sIdxBlk, fv, wQ[qn - 32 + lane],
+                                                         true);
+                            qn -= 32;
+                            __syncwarp();
                         }
                     }
                 }

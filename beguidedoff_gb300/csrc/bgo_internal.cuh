@@ -316,6 +316,8 @@ bool build_filter_tables(const FamilyDesc *fams, int n_fams, const GuideRec *rec
 uint32_t filter_tab_bytes(int K);
 // dynamic shared memory of a prefiltered form besides the survivor index
 size_t filter_smem_fixed_bytes(int K, int chunk_sites);
+// dynamic shared memory a prefiltered launch may take
+size_t filter_smem_limit();
 int launch_filter_kernel(const ScanParams &p, const FilterArgs &fa, int sm_count, int chunk_sites,
                          cudaStream_t s);
 int launch_mask_kernel(const ScanParams &p, const MaskArgs &ma, int sm_count, int ctas_per_sm,

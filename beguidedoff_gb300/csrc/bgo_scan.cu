@@ -905,7 +905,7 @@ static int scan_launch(bgo_engine *engine, const bgo_plan *plan, const bgo_genom
                 }
                 fa.idx_smem_bytes =
                     fits16 && filter_smem_fixed_bytes(max_mismatches, chunk) + need <=
-                                  (size_t)(227 * 1024)
+                                  filter_smem_limit()
                         ? (int32_t)need
                         : 0;
                 BGO_CUDA(cudaMemsetAsync(engine->d_work, 0, sizeof(uint32_t) * (size_t)(g1 - g0), s));

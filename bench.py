@@ -41,10 +41,10 @@ UNIT = "cmp/s"
 # form, 4,096-position chunks) of the plain workload at 300 Mbp, from ncu
 # (profiles/scan_filter_kernel_ngg100_300mbp.md); traffic grows with the
 # genome, so the line scales it to the run's length
-NCU_TRAFFIC_PLAIN = (300_000_000, 226.679808e6 + 6.000128e6)
+NCU_TRAFFIC_PLAIN = (300_000_000, 225.629440e6 + 3.540480e6)
 # the same capture's integer-pipe figures: the kernel is issue-bound, so these
 # are its roofline in the integer-ALU sense
-NCU_INT_PLAIN = {"issue_active_frac": 0.605, "alu_pipe_active_frac": 0.529,
+NCU_INT_PLAIN = {"issue_active_frac": 0.693, "alu_pipe_active_frac": 0.603,
                  "warps_active_frac": 0.375,
                  "source": "ncu smsp__issue_active, sm__pipe_alu_cycles_active, "
                            "sm__warps_active (pct of peak, active cycles) at 300 Mbp, "

@@ -272,6 +272,70 @@ def test_prefilter_headline_shape_equals_oracle(k, chunk):
         f.close()
 
 
+def _write_base(genome, ci, p, v, n=False):
+    """Base code v (A0 C1 G2 T3) at forward position p of chromosome ci, its
+    complement at the mirrored reverse-complement position, and the N bit."""
+    fwd, rc, nm = genome["genome_forward"], genome["genome_rc"], genome["n_mask"]
+    off, ln = int(genome["chrom_offsets"][ci]), int(genome["chrom_lengths"][ci])
+    fwd[p >> 4] = (fwd[p >> 4] & ~np.uint32(3 << ((p & 15) * 2))) | np.uint32(v << ((p & 15) * 2))
+    q = off + ln - 1 - (p - off)
+    rc[q >> 4] = (rc[q >> 4] & ~np.uint32(3 << ((q & 15) * 2))) | np.uint32((3 - v) << ((q & 15) * 2))
+    bit = np.uint8(1 << (7 - (p & 7)))
+    nm[p >> 3] = (nm[p >> 3] | bit) if n else (nm[p >> 3] & np.uint8(~bit & 0xFF))
+
+
+@pytest.mark.parametrize("chunk", [2048, 4096])
+def test_prefilter_n_summary_boundaries_equal_oracle(chunk):
+    """The prefiltered form learns whether a chunk holds an N from the
+    strand's N summary (one bit per 1,024 positions, the chunk's halo
+    included) and reads N words from global memory.  Sites planted across
+    1,024-position boundaries of either strand, with a single N inside the
+    window at or just past the boundary (the guide's base there is the base
+    an N is stored as, so only the N correction tells the hit's mismatches):
+    keys equal the oracle's."""
+    genome, rng = _random_genome(900 + chunk, [300_000, 200_003])
+    code = {"A": 0, "C": 1, "G": 2, "T": 3}
+    off0, ln0 = int(genome["chrom_offsets"][0]), int(genome["chrom_lengths"][0])
+    seqs = []
+    for b in range(1024, ln0 - 1024, 1024 * 7):
+        for strand in (0, 1):
+            j = int(rng.integers(0, 3))           # the N at boundary + j
+            d = int(rng.integers(1, 20))          # window start = boundary + j - d
+            guide = list("".join(rng.choice(list("ACGT"), 20)))
+            # the guide's base at the N: A on the forward strand (N is stored
+            # as A there), T on the reverse strand (N reads as T)
+            guide[d] = "A" if strand == 0 else "T"
+            guide = "".join(guide)
+            seqs.append(guide)
+            site = guide + "AGG"
+            if strand == 0:
+                start = off0 + b + j - d
+                for k, c in enumerate(site):
+                    _write_base(genome, 0, start + k, code[c])
+                _write_base(genome, 0, off0 + b + j, 0, n=True)
+            else:
+                # reverse-strand position r maps to forward off0 + ln0 - 1 - r
+                r0 = b + j - d
+                for k, c in enumerate(site):
+                    _write_base(genome, 0, off0 + ln0 - 1 - (r0 + k), 3 - code[c])
+                _write_base(genome, 0, off0 + ln0 - 1 - (b + j), 0, n=True)
+    pams = ["NGG"] * len(seqs)
+    for k in (1, 4):
+        exp = oracle_keys(genome, seqs, pams, k)
+        f = beguidedoff(None, max_mismatches=k, genome_data=genome)
+        try:
+            plan = f._plan(seqs, pams)
+            plan.set_tuning(chunk, 0, 0, 0, 0, 1, 0, 0, 1)
+            got = f._engine.scan(plan, f._strands, [0, 3], k, 2)
+            assert got.size == exp.size and np.array_equal(got, exp), k
+            # every planted site is a hit whose N counts as a mismatch
+            mm = (exp & 63).astype(np.int64)
+            assert (mm >= 1).sum() >= len(seqs)
+            plan.close()
+        finally:
+            f.close()
+
+
 @pytest.mark.parametrize("tune", [(2048, 0, 0, 0, 0, 1, 0, 0, 1), (4096, 0, 0, 0, 0, 1, 0, 0, 1),
                                   (0, 0, 0, 0, 1, 1), (0, 0, 0, 0, 3, 0), None])
 def test_overflow_rescans_only_dropped_granules(tune):
