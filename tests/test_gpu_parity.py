@@ -285,14 +285,14 @@ def _write_base(genome, ci, p, v, n=False):
 
 
 @pytest.mark.parametrize("chunk", [2048, 4096])
-def test_prefilter_n_summary_boundaries_equal_oracle(chunk):
-    """The prefiltered form learns whether a chunk holds an N from the
-    strand's N summary (one bit per 1,024 positions, the chunk's halo
-    included) and reads N words from global memory.  Sites planted across
+def test_prefilter_n_at_chunk_boundaries_equal_oracle(chunk):
+    """The prefiltered form skips the N correction in chunks whose staged N
+    words (the halo included) are all zero.  Sites planted across
     1,024-position boundaries of either strand, with a single N inside the
-    window at or just past the boundary (the guide's base there is the base
-    an N is stored as, so only the N correction tells the hit's mismatches):
-    keys equal the oracle's."""
+    window at or just past the boundary, so that for a chunk boundary the N
+    lies in the previous chunk's halo only (the guide's base there is the
+    base an N is stored as, so only the N correction tells the hit's
+    mismatches): keys equal the oracle's."""
     genome, rng = _random_genome(900 + chunk, [300_000, 200_003])
     code = {"A": 0, "C": 1, "G": 2, "T": 3}
     off0, ln0 = int(genome["chrom_offsets"][0]), int(genome["chrom_lengths"][0])
