@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                     }
                 }
             };
-            int total = 0, off0 = 0, cnt = 0;
+            int total = 0;
 #pragma unroll 1
             for (int pass_i = 0; pass_i < C::kPasses; ++pass_i) {
                 // a further pass only while listed positions remain (the
@@ -486,17 +486,33 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                 if (pass_i > 0 && pass_i * C::kListCap >= total) break;
                 uint32_t pass[C::kRows];
                 pam_pass(pass);
-                if (pass_i == 0) {
+                // The list is row-major: row u's positions of lanes 0..31, then
+                // row u + 1's.  A round's lanes then read window words of
+                // neighbouring lanes' words, which lie in different banks (a
+                // lane-major list put a round's positions in one lane's words,
+                // all in the same bank).  Row offsets: one warp scan per two
+                // rows, the two counts in 16-bit halves (sums <= 1,024).
+                int rowoff[C::kRows];
+                {
+                    int base = 0;
 #pragma unroll
-                    for (int u = 0; u < C::kRows; ++u) cnt += __popc(pass[u]);
-                    int incl = cnt;
+                    for (int h = 0; h < C::kRows / 2; ++h) {
+                        const uint32_t pk = (uint32_t)__popc(pass[2 * h]) |
+                                            ((uint32_t)__popc(pass[2 * h + 1]) << 16);
+                        uint32_t incl = pk;
 #pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                        if (lane >= o) incl += v;
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                            if (lane >= o) incl += v;
+                        }
+                        const uint32_t tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
+                        const uint32_t ex = incl - pk;
+                        rowoff[2 * h] = base + (int)(ex & 0xFFFFu);
+                        base += (int)(tot & 0xFFFFu);
+                        rowoff[2 * h + 1] = base + (int)(ex >> 16);
+                        base += (int)(tot >> 16);
                     }
-                    total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-                    off0 = incl - cnt;
+                    if (pass_i == 0) total = base;
                 }
                 const int lo = pass_i * C::kListCap;
                 if (lo >= total) break;
@@ -505,9 +521,9 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                 // positions (the order within a lane's word is irrelevant: each
                 // word is walked from its highest passing bit)
                 if (total <= C::kListCap) {
-                    uint16_t *out = wList + off0;
 #pragma unroll
                     for (int u = 0; u < C::kRows; ++u) {
+                        uint16_t *out = wList + rowoff[u];
                         uint32_t m = pass[u];
                         const uint32_t wb = 32u * (uint32_t)(u * 32 + lane) + 31u;
                         // two steps without a loop branch (most words hold at
@@ -525,10 +541,10 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                             *out++ = (uint16_t)(wb - z);
                         }
                     }
-                } else if (off0 + cnt > lo && off0 < lo + n_list) {
-                    int off = off0 - lo;
+                } else {
 #pragma unroll
                     for (int u = 0; u < C::kRows; ++u) {
+                        int off = rowoff[u] - lo;
                         uint32_t m = pass[u];
                         const uint32_t wb = 32u * (uint32_t)(u * 32 + lane) + 31u;
                         while (m) {

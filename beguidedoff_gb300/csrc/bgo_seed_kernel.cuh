@@ -215,17 +215,34 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, SeedCta<MINB>::kPerSm
                                        : ~(((h ^ m.x) & m.y) | ((l ^ m.z) & m.w));
                 }
             }
-            int cnt = 0;
+            // The list is row-major (row u's positions of lanes 0..31, then row
+            // u + 1's), so that a round's lanes read window words of
+            // neighbouring lanes' words, in different banks.  Row offsets: one
+            // warp scan per two rows, the counts in 16-bit halves.
+            int rowoff[C::kRows];
+            int total = 0;
 #pragma unroll
-            for (int u = 0; u < C::kRows; ++u) cnt += __popc(pass[u]);
-            int incl = cnt;
+            for (int h = 0; h < (C::kRows + 1) / 2; ++h) {
+                // (the second row's index is clamped so that the one-row form
+                // has no out-of-range access even in its dead branch)
+                const bool two = 2 * h + 1 < C::kRows;
+                const uint32_t pk = (uint32_t)__popc(pass[2 * h]) |
+                                    (two ? (uint32_t)__popc(pass[two ? 2 * h + 1 : 0]) << 16 : 0u);
+                uint32_t incl = pk;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                if (lane >= o) incl += v;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                const uint32_t tot = __shfl_sync(0xFFFFFFFFu, incl, 31);
+                const uint32_t ex = incl - pk;
+                rowoff[2 * h] = total + (int)(ex & 0xFFFFu);
+                total += (int)(tot & 0xFFFFu);
+                if (two) {
+                    rowoff[two ? 2 * h + 1 : 0] = total + (int)(ex >> 16);
+                    total += (int)(tot >> 16);
+                }
             }
-            const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            const int off0 = incl - cnt;
             // the family's bucket tables and entry bases, held in registers
             uint32_t seg_off[S], seg_ent[S];
             {
@@ -245,9 +262,9 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, SeedCta<MINB>::kPerSm
                 // list positions [lo, lo + n_list) of the chunk's passing positions
                 // (one pass, the common case: every lane lists all of its own)
                 if (C::kPasses == 1 || total <= C::kListCap) {
-                    int off = off0;
 #pragma unroll
                     for (int u = 0; u < C::kRows; ++u) {
+                        int off = rowoff[u];
                         uint32_t m = pass[u];
                         while (m) {
                             const int j = __ffs(m) - 1;
@@ -255,10 +272,10 @@ __global__ void __launch_bounds__(SeedCta<MINB>::kThreads, SeedCta<MINB>::kPerSm
                             wList[off++] = (uint16_t)(32 * (u * 32 + lane) + j);
                         }
                     }
-                } else if (off0 + cnt > lo && off0 < lo + n_list) {
-                    int off = off0 - lo;
+                } else {
 #pragma unroll
                     for (int u = 0; u < C::kRows; ++u) {
+                        int off = rowoff[u] - lo;
                         uint32_t m = pass[u];
                         while (m) {
                             const int j = __ffs(m) - 1;
