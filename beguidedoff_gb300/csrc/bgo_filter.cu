@@ -42,15 +42,20 @@
 // survivors read the index (with full guide planes per entry) from global
 // memory (L1/L2).
 //
-// Work.  One persistent 768-thread CTA per SM.  Per launch family the warps
+// Work.  One persistent 896-thread CTA (28 warps) per SM.  Per launch family the warps
 // take the first three quarters of the chunks in a static grid stride and
 // claim the rest in runs of two from a per-family counter (atomicAdd), so the
 // families of a mixed plan share one launch without a tail per family; the
 // CTA loads the next family's filter tables after all its warps are done with
 // the previous one (a CTA barrier per family).  Chunks of 2,048 or 4,096
-// positions are copied into the warp's double buffer by one lane with three
-// 1-D bulk copies (cp.async.bulk, one per plane) completing on an mbarrier;
-// the wait is bounded and reports BGO_ERR_TIMEOUT through the engine.
+// positions are copied into the warp's double buffer by one lane with two
+// 1-D bulk copies (cp.async.bulk, the H and L planes) completing on an
+// mbarrier; the wait is bounded and reports BGO_ERR_TIMEOUT through the
+// engine.  The N plane is not staged: the strand's N summary (one bit per
+// 1,024 positions, built when the strand is uploaded) tells whether a chunk
+// or its halo holds an N, and only then do the chunk's survivors read their
+// N words from global memory.  That leaves room for 28 warps' slices beside
+// the tables and the survivor index.
 //
 // This translation unit instantiates the 2,048-position form with the index
 // in shared memory; bgo_filter_2k_g.cu, bgo_filter_4k.cu and bgo_filter_4k_s.cu

@@ -16,7 +16,7 @@
 namespace bgo {
 
 #ifndef BGO_FILTER_THREADS
-#define BGO_FILTER_THREADS 768
+#define BGO_FILTER_THREADS 896
 #endif
 constexpr int kFilterThreads = BGO_FILTER_THREADS;  // one CTA per SM
 constexpr int kFilterWarps = kFilterThreads / 32;
@@ -39,7 +39,7 @@ constexpr unsigned long long kCopyWaitNs = 2000000000ull;
 // static shared memory of the kernel (counters, the chunk-order start and
 // the warps' index views) stays below this; the dynamic block takes the rest
 // of the 227 KB a CTA may hold
-constexpr int kFilterStaticSmem = 1024;
+constexpr int kFilterStaticSmem = 2048;
 // dynamic shared memory a prefiltered form may take
 constexpr int kFilterSmemLimit = 227 * 1024 - kFilterStaticSmem;
 
@@ -65,7 +65,9 @@ struct FiltT {
 };
 
 // Per-warp shared-memory slice for chunks of CH positions: two chunk buffers
-// (H, L, N planes, each CH/32 + 4 words), the compacted list of PAM-passing
+// (H and L planes, each CH/32 + 4 words; the N plane stays in global memory,
+// read only for survivors of chunks whose N summary is set), the compacted
+// list of PAM-passing
 // positions, the survivor queue (plus one slot that absorbs the stores of
 // lanes without a survivor) and the two chunk buffers' mbarriers.
 template <int CH>
@@ -73,7 +75,7 @@ struct FiltChunk {
     static constexpr int kRows = CH / 1024;     // 32-position words per lane
     static constexpr int kWords = CH / 32 + 4;  // + halo, a multiple of 4 words
     static constexpr uint32_t kPlaneBytes = kWords * 4u;
-    static constexpr size_t kBuf = 3 * (size_t)kPlaneBytes;
+    static constexpr size_t kBuf = 2 * (size_t)kPlaneBytes;
     static constexpr int kListCap = CH >= 4096 ? 512 : 1024;
     static constexpr int kPasses = CH / kListCap;
     static constexpr size_t kListOff = 2 * kBuf;
@@ -278,9 +280,9 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
         const uint32_t *cl = *(const uint32_t *volatile *)&sChunkList;
         return cl ? (int)cl[i] : i;
     };
-    // Copies chunk c's words [c*CH/32, c*CH/32 + kWords) of the three planes
+    // Copies chunk c's words [c*CH/32, c*CH/32 + kWords) of the H and L planes
     // into buffer b (the planes are padded so that the copy never leaves them,
-    // and zero beyond total_bp).  One lane issues the three bulk copies.
+    // and zero beyond total_bp).  One lane issues the two bulk copies.
     auto issue = [&](int c, int b) {
         if (lane == 0) {
             const bool second = c >= chunks0;
@@ -291,10 +293,9 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
             // the warp's reads of this buffer (generic proxy) come before the
             // copy's writes (async proxy)
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-            mbar_expect_tx(bar, 3u * C::kPlaneBytes);
+            mbar_expect_tx(bar, 2u * C::kPlaneBytes);
             bulk_g2s(dst, sd.H + w0, C::kPlaneBytes, bar);
             bulk_g2s(dst + C::kPlaneBytes, sd.L + w0, C::kPlaneBytes, bar);
-            bulk_g2s(dst + 2u * C::kPlaneBytes, sd.N + w0, C::kPlaneBytes, bar);
         }
     };
     // Chunk order of a warp: the first kStaticQuarters/4 of the chunks in a
@@ -419,17 +420,21 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
             }
             const uint32_t *wH = reinterpret_cast<const uint32_t *>(slice + buf * C::kBuf);
             const uint32_t *wL = wH + C::kWords;
-            const uint32_t *wN = wL + C::kWords;
             const int chunk = chunk_at(cur);
             const bool second = chunk >= chunks0;
             const uint32_t lc = (uint32_t)(second ? chunk - chunks0 : chunk);
             const uint32_t total_bp =
                 (uint32_t)(second ? p.strand[1].total_bp : p.strand[0].total_bp);
-            int has_n = second ? p.strand[1].has_n : p.strand[0].has_n;
-            if (has_n) {
-                uint32_t nw = 0;
-                for (int i = lane; i < C::kWords; i += 32) nw |= wN[i];
-                has_n = __any_sync(0xFFFFFFFFu, nw != 0u);
+            // an N in the chunk's words [lc * CH/32, + kWords): summary bits
+            // [g0, g0 + CH/1024 + 1) of groups of 32 words
+            bool has_n = false;
+            {
+                const uint32_t *ns = second ? p.strand[1].nsum : p.strand[0].nsum;
+                if (ns) {
+                    const uint32_t g0 = lc * (uint32_t)(CH / 1024);
+                    const uint32_t lo = __ldg(ns + (g0 >> 5)), hi = __ldg(ns + (g0 >> 5) + 1);
+                    has_n = (sfshr(lo, hi, g0 & 31u) & ((2u << (CH / 1024)) - 1u)) != 0u;
+                }
             }
             const uint32_t strand_bit = second ? 0x80000000u : 0u;
             // positions [0, lim) of this chunk are scanned (total_bp - 26
@@ -610,11 +615,16 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                             const uint32_t s = sv[v];
                             uint32_t n20g = 0;
                             if (has_n) {
+                                // the chunk's N words, from global memory
+                                const uint32_t *gN =
+                                    (strand_bit ? p.strand[1].N : p.strand[0].N) + (base32 >> 5);
                                 const uint32_t wo = s + win_off;
-                                const uint32_t n26 =
-                                    sfshr(wN[s >> 5], wN[(s >> 5) + 1], s & 31u) & 0x3FFFFFFu;
-                                const uint32_t n20 =
-                                    sfshr(wN[wo >> 5], wN[(wo >> 5) + 1], wo & 31u) & 0xFFFFFu;
+                                const uint32_t n26 = sfshr(__ldg(gN + (s >> 5)),
+                                                           __ldg(gN + (s >> 5) + 1), s & 31u) &
+                                                     0x3FFFFFFu;
+                                const uint32_t n20 = sfshr(__ldg(gN + (wo >> 5)),
+                                                           __ldg(gN + (wo >> 5) + 1), wo & 31u) &
+                                                     0xFFFFFu;
                                 n20g = n26 ? n20 : 0u;
                             }
                             // a lane without a survivor stores into the spare slot

@@ -52,6 +52,27 @@ __global__ void planes_from_packed_kernel(const uint32_t *__restrict__ packed, i
     planes[2 * plane_words + w] = N & keep;
 }
 
+// N summary of a strand: thread g ORs N-plane words [32g, 32g + 32); one
+// warp ballot packs 32 groups into a word.
+__global__ void nsum_kernel(const uint32_t *__restrict__ nplane, int64_t plane_words,
+                            uint32_t *__restrict__ nsum, int64_t nsum_words) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t any = 0;
+    const int64_t w0 = g * kNSumGroup;
+    for (int i = 0; i < kNSumGroup; ++i)
+        if (w0 + i < plane_words) any |= nplane[w0 + i];
+    const unsigned bits = __ballot_sync(0xFFFFFFFFu, any != 0u);
+    if ((threadIdx.x & 31) == 0 && (g >> 5) < nsum_words) nsum[g >> 5] = bits;
+}
+
+static cudaError_t build_nsum(bgo_genome *g, cudaStream_t s) {
+    if (!g->d_nsum) return cudaSuccess;
+    const int64_t threads = 32 * g->nsum_words;
+    nsum_kernel<<<(unsigned)ceil_div(threads, 256), 256, 0, s>>>(
+        g->d_planes + 2 * g->plane_words, g->plane_words, g->d_nsum, g->nsum_words);
+    return cudaGetLastError();
+}
+
 }  // namespace bgo
 
 extern "C" int bgo_genome_create(const uint32_t *packed, int64_t n_words, int64_t total_bp,
@@ -82,7 +103,11 @@ extern "C" int bgo_genome_create(const uint32_t *packed, int64_t n_words, int64_
     uint32_t *d_packed = nullptr;
     uint8_t *d_mask = nullptr;
     int rc = BGO_OK;
+    g->d_nsum = nullptr;
+    g->nsum_words = g->has_n ? nsum_words_for(g->plane_words) : 0;
     cudaError_t e = cudaMalloc(&g->d_planes, (size_t)g->bytes);
+    if (e == cudaSuccess && g->has_n)
+        e = cudaMalloc(&g->d_nsum, sizeof(uint32_t) * (size_t)g->nsum_words);
     if (e == cudaSuccess) e = cudaMalloc(&d_packed, (size_t)n_words * sizeof(uint32_t));
     if (e == cudaSuccess && g->has_n) e = cudaMalloc(&d_mask, (size_t)n_mask_bytes);
     if (e == cudaSuccess)
@@ -98,12 +123,14 @@ extern "C" int bgo_genome_create(const uint32_t *packed, int64_t n_words, int64_
             g->d_planes);
         e = cudaGetLastError();
     }
+    if (e == cudaSuccess) e = build_nsum(g, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) rc = cuda_fail(e, "bgo_genome_create");
     if (d_packed) cudaFree(d_packed);
     if (d_mask) cudaFree(d_mask);
     if (rc != BGO_OK) {
         if (g->d_planes) cudaFree(g->d_planes);
+        if (g->d_nsum) cudaFree(g->d_nsum);
         delete g;
         return rc;
     }
@@ -144,6 +171,7 @@ extern "C" int bgo_genome_upload(bgo_genome *g, const uint32_t *packed, int64_t 
         d_packed, n_words, d_mask, g->has_n ? n_mask_bytes : 0, g->total_bp, g->plane_words,
         g->d_planes);
     BGO_CUDA(cudaGetLastError());
+    BGO_CUDA(build_nsum(g, s));
     return BGO_OK;
 }
 
@@ -151,6 +179,7 @@ extern "C" int bgo_genome_destroy(bgo_genome *genome) {
     if (!genome) return BGO_OK;
     cudaSetDevice(genome->device);
     if (genome->d_stage) cudaFree(genome->d_stage);
+    if (genome->d_nsum) cudaFree(genome->d_nsum);
     cudaError_t e = genome->d_planes ? cudaFree(genome->d_planes) : cudaSuccess;
     delete genome;
     if (e != cudaSuccess) return bgo::cuda_fail(e, "bgo_genome_destroy");

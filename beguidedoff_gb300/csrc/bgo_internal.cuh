@@ -46,6 +46,9 @@ struct GuideRec {
 
 struct StrandDesc {
     const uint32_t *H, *L, *N;
+    // N summary: bit g set iff N-plane words [32g, 32g + 32) hold an N;
+    // nullptr for a strand without an N mask
+    const uint32_t *nsum;
     int64_t total_bp;
     int64_t n_tiles;
     int32_t has_n;
@@ -226,6 +229,14 @@ inline int64_t tiles_for(int64_t total_bp) {
 // plain kernel and every 16-byte-aligned chunk copy of the segment-indexed
 // and prefiltered kernels ([c*64, c*64 + 68) words for 2,048-position chunks,
 // [c*128, c*128 + 132) for 4,096) is inside the buffer.
+// N-plane words per bit of a strand's N summary (1,024 positions)
+constexpr int kNSumGroup = 32;
+// words of the N summary of a strand with `plane_words` plane words (one
+// spare word, so that a reader may always load two consecutive words)
+inline int64_t nsum_words_for(int64_t plane_words) {
+    return (plane_words + 32 * kNSumGroup - 1) / (32 * kNSumGroup) + 1;
+}
+
 inline int64_t plane_words_for(int64_t total_bp) {
     int64_t t = tiles_for(total_bp);
     int64_t need = t * (kTileSites / 32) + kTileWords;
@@ -248,6 +259,8 @@ struct bgo_genome {
     int32_t has_n;
     int64_t plane_words;
     uint32_t *d_planes;  // [3][plane_words]
+    uint32_t *d_nsum;    // N summary (StrandDesc::nsum), nsum_words words; null without N
+    int64_t nsum_words;
     int64_t bytes;
     unsigned char *d_stage = nullptr;  // packed words + N mask of bgo_genome_upload
     size_t stage_bytes = 0;

@@ -176,6 +176,7 @@ extern "C" int bgo_scan_noalloc(const bgo_genome *const *strands, const int32_t 
             d.H = g->d_planes;
             d.L = g->d_planes + g->plane_words;
             d.N = g->d_planes + 2 * g->plane_words;
+            d.nsum = g->d_nsum;
             d.total_bp = g->total_bp;
             d.n_tiles = tiles_for(g->total_bp);
             d.has_n = g->has_n;

@@ -486,6 +486,7 @@ static void fill_strand(StrandDesc &d, const bgo_genome *g, int32_t n_encoded, i
     d.H = g->d_planes;
     d.L = g->d_planes + g->plane_words;
     d.N = g->d_planes + 2 * g->plane_words;
+    d.nsum = g->d_nsum;
     d.total_bp = g->total_bp;
     d.n_tiles = tiles_for(g->total_bp);
     d.has_n = g->has_n;

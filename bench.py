@@ -41,11 +41,11 @@ UNIT = "cmp/s"
 # form, 4,096-position chunks) of the plain workload at 300 Mbp, from ncu
 # (profiles/scan_filter_kernel_ngg100_300mbp.md); traffic grows with the
 # genome, so the line scales it to the run's length
-NCU_TRAFFIC_PLAIN = (300_000_000, 225.629440e6 + 3.540480e6)
+NCU_TRAFFIC_PLAIN = (300_000_000, 151.840000e6 + 5.714688e6)
 # the same capture's integer-pipe figures: the kernel is issue-bound, so these
 # are its roofline in the integer-ALU sense
-NCU_INT_PLAIN = {"issue_active_frac": 0.693, "alu_pipe_active_frac": 0.603,
-                 "warps_active_frac": 0.375,
+NCU_INT_PLAIN = {"issue_active_frac": 0.766, "alu_pipe_active_frac": 0.669,
+                 "warps_active_frac": 0.437,
                  "source": "ncu smsp__issue_active, sm__pipe_alu_cycles_active, "
                            "sm__warps_active (pct of peak, active cycles) at 300 Mbp, "
                            "scan_filter_kernel<4, 4096, 1>"}
@@ -755,8 +755,16 @@ def bench_ours(args, ws, rank, local):
     per_launch_s = (total_ms / 1e3) / max(1, launches)
     pairs_per_launch = pairs / max(1, launches // args.steps) if args.mode == 0 else pairs
     achieved = pairs / (total_ms / 1e3 / args.steps) / 1e9
-    # algorithmic bytes: the H, L and N planes of both strands, read once
-    plane_bytes = len(f._strands) * 3 * 4 * ((total + 31) // 32)
+    # algorithmic bytes: the H, L and N planes of both strands, read once; the
+    # prefiltered form in one launch streams H and L only, plus the strands'
+    # N summaries (one bit per 1,024 positions; the N words that survivors of
+    # chunks with an N read are data-dependent and not counted)
+    tune_now = getattr(plan, "tuning", None) or {}
+    words = (total + 31) // 32
+    if tune_now.get("prefilter") and not tune_now.get("split_families"):
+        plane_bytes = len(f._strands) * (2 * 4 * words + 4 * ((words + 1023) // 1024 + 1))
+    else:
+        plane_bytes = len(f._strands) * 3 * 4 * words
     hbm_peak = None
     try:
         hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
