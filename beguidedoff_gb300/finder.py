@@ -98,10 +98,13 @@ def _decode_strings(seq: np.ndarray, pam: np.ndarray, plen: np.ndarray):
     n = seq.shape[0]
     if n == 0:
         return np.zeros(0, dtype=object), np.zeros(0, dtype=object)
-    s = np.ascontiguousarray(_ASCII[seq]).view("S20").ravel().astype("U20").astype(object)
-    pa = _ASCII[pam]
-    pa[np.arange(6)[None, :] >= plen[:, None]] = 0   # bytes strings end at the first NUL
-    p = np.ascontiguousarray(pa).view("S6").ravel().astype("U6").astype(object)
+    # one decode of all the bytes, then slices (cheaper than a numpy string
+    # dtype round trip at the sizes a table has)
+    sr = _ASCII[seq].tobytes().decode("ascii")
+    pr = _ASCII[pam].tobytes().decode("ascii")
+    s = np.array([sr[20 * i:20 * i + 20] for i in range(n)] + [None], dtype=object)[:-1]
+    p = np.array([pr[6 * i:6 * i + k] for i, k in enumerate(plen.tolist())] + [None],
+                 dtype=object)[:-1]
     return s, p
 
 
@@ -142,12 +145,18 @@ def _guide_bases(seqs: List[str]) -> np.ndarray:
     return gb
 
 
-def _per_unique(values: np.ndarray, fn) -> np.ndarray:
-    """fn applied once per distinct value, spread back (an object array)."""
+def _per_unique(values: np.ndarray, fn, cache: Optional[dict] = None) -> np.ndarray:
+    """fn applied once per distinct value, spread back (an object array).
+    ``cache`` is fn's memo: small arrays are mapped through it in one pass,
+    calling fn only for values it does not hold yet."""
     if values.size == 0:
         return np.zeros(0, dtype=object)
     if values.size <= 4096:  # fn is memoised: a direct pass is cheaper than unique
-        return np.array([fn(v) for v in values.tolist()] + [None], dtype=object)[:-1]
+        vals = values.tolist()
+        out = list(map(cache.get, vals)) if cache is not None else [None] * len(vals)
+        if None in out:
+            out = [fn(v) if o is None else o for o, v in zip(out, vals)]
+        return np.array(out + [None], dtype=object)[:-1]
     uniq, inv = np.unique(values, return_inverse=True)
     mapped = np.array([fn(v) for v in uniq.tolist()] + [None], dtype=object)[:-1]
     return mapped[inv.ravel()]
@@ -617,7 +626,7 @@ class beguidedoff:
         editors = [guides[i].base_editor or "" for i in rows_in.tolist()]
         below = [bid.get(guides[i].guide_id, 0) for i in rows_in.tolist()]
         seq_s, pam_s = _decode_strings(seq[idx], pam[idx], plen[idx])
-        mpos = _per_unique(mmask[idx], _mismatch_positions)
+        mpos = _per_unique(mmask[idx], _mismatch_positions, _MM_POSITIONS)
         cols = {
             "guide_rna_sequence": plan_seq[row[idx]],
             "base_editor": np.repeat(np.array(editors, dtype=object), sizes),
@@ -629,7 +638,7 @@ class beguidedoff:
             "ot_pam": np.array(pam_s, dtype=object),
             "n_mismatches": mm[idx].astype(np.int64),
             "mismatch_positions": np.array(mpos, dtype=object),
-            "score": _per_unique(score[idx], _round6).astype(np.float64),
+            "score": _per_unique(score[idx], _round6, _ROUND6).astype(np.float64),
             "n_offtargets_below_threshold": np.repeat(np.array(below, dtype=np.int64), sizes),
         }
         t = Table(cols, COLUMNS)

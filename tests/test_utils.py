@@ -108,3 +108,26 @@ def test_base_editing_known_answers():
     assert B.has_editable_base(seq, "CBE", 4, 8)
     with pytest.raises(ValueError):
         B.editable_base_in_window(seq, "XBE", 4, 8)
+
+
+def test_table_string_helpers():
+    """The device-path table's window and PAM strings, mismatch-position
+    strings and rounded scores equal their plain definitions."""
+    from beguidedoff_gb300 import finder as F
+
+    rng = np.random.default_rng(3)
+    seq = rng.integers(0, 4, (40, 20)).astype(np.uint8)
+    pam = rng.integers(0, 4, (40, 6)).astype(np.uint8)
+    plen = rng.integers(1, 7, 40)
+    s, p = F._decode_strings(seq, pam, plen)
+    for i in range(40):
+        assert s[i] == "".join("ACGT"[b] for b in seq[i])
+        assert p[i] == "".join("ACGT"[b] for b in pam[i][:plen[i]])
+    masks = rng.integers(0, 1 << 20, 300).astype(np.int64)
+    mp = F._per_unique(masks, F._mismatch_positions, F._MM_POSITIONS)
+    for m, got in zip(masks.tolist(), mp.tolist()):
+        assert got == ",".join(str(i + 1) for i in range(20) if (m >> i) & 1)
+    vals = S.cctop_from_masks(masks)
+    r6 = F._per_unique(vals, F._round6, F._ROUND6).astype(np.float64)
+    assert all(a == round(b, 6) for a, b in zip(r6.tolist(), vals.tolist()))
+    assert F._decode_strings(seq[:0], pam[:0], plen[:0])[0].size == 0
