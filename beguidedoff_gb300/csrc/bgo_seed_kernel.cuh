@@ -59,9 +59,11 @@ struct SegT {
 // The full check of a candidate whose raw count cm <= K, found through
 // region j: emits the hit if j is its first region with <= TOL mismatches
 // and it stays within K after the N correction.  Returns true when the hit
-// did not fit the hit buffer (the caller marks its granule).
+// did not fit the hit buffer (the caller marks its granule).  Inlined: as a
+// call, its calling convention spilled registers of every kernel that uses it
+// (the prefiltered kernel at 72 registers spilled 56 bytes; inlined, none).
 template <int K, int TOL>
-__device__ __noinline__ bool finish_candidate(const ScanParams &p, uint32_t m, int cm, uint2 e,
+__device__ __forceinline__ bool finish_candidate(const ScanParams &p, uint32_t m, int cm, uint2 e,
                                               uint32_t idx, int j, uint32_t n20g, uint32_t ne,
                                               uint64_t slot, uint64_t pos, uint32_t gbeg) {
     using G = SegT<K, TOL>;
