@@ -52,17 +52,20 @@ __global__ void planes_from_packed_kernel(const uint32_t *__restrict__ packed, i
     planes[2 * plane_words + w] = N & keep;
 }
 
-// N summary of a strand: thread g ORs N-plane words [32g, 32g + 32); one
-// warp ballot packs 32 groups into a word.
+// N summary of a strand: warp v builds summary word v, whose bit k covers
+// N-plane words [32 (32 v + k), + 32): in step k lane i reads word
+// 32 (32 v + k) + i (the warp's 32 loads coalesced) and the warp votes.
 __global__ void nsum_kernel(const uint32_t *__restrict__ nplane, int64_t plane_words,
                             uint32_t *__restrict__ nsum, int64_t nsum_words) {
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t any = 0;
-    const int64_t w0 = g * kNSumGroup;
-    for (int i = 0; i < kNSumGroup; ++i)
-        if (w0 + i < plane_words) any |= nplane[w0 + i];
-    const unsigned bits = __ballot_sync(0xFFFFFFFFu, any != 0u);
-    if ((threadIdx.x & 31) == 0 && (g >> 5) < nsum_words) nsum[g >> 5] = bits;
+    const int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    uint32_t bits = 0;
+    for (int k = 0; k < 32; ++k) {
+        const int64_t w = (v * 32 + k) * kNSumGroup + lane;
+        const uint32_t x = (v < nsum_words && w < plane_words) ? nplane[w] : 0u;
+        if (__any_sync(0xFFFFFFFFu, x != 0u)) bits |= 1u << k;
+    }
+    if (lane == 0 && v < nsum_words) nsum[v] = bits;
 }
 
 static cudaError_t build_nsum(bgo_genome *g, cudaStream_t s) {
