@@ -531,10 +531,12 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                         uint16_t *out = wList + rowoff[u];
                         uint32_t m = pass[u];
                         const uint32_t wb = 32u * (uint32_t)(u * 32 + lane) + 31u;
-                        // two steps without a loop branch (most words hold at
-                        // most two passing positions), then the rest
+                        // three steps without a loop branch (most words hold at
+                        // most three passing positions; the loop after them runs
+                        // as long as the warp's fullest word needs), then the
+                        // rest
 #pragma unroll
-                        for (int it = 0; it < 2; ++it) {
+                        for (int it = 0; it < 3; ++it) {
                             const uint32_t z = __clz(m);
                             if (m) *out = (uint16_t)(wb - z);
                             out += m ? 1 : 0;
