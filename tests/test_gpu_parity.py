@@ -548,7 +548,10 @@ def test_five_prime_pams_every_form_equals_oracle():
     try:
         plan = _native.Plan(f._engine, gv, pm, pl, p3)
         forms = [(0, ()), (1, ()), (2, ()), (2, (0, 0, 0, 1)), (2, (0, 0, 0, 0, 0, 1)),
-                 (2, (1024, 0, 0, 1, 4, 0, 2)), (2, (0, 0, 0, 0, 0, 0, 0, 1)), (3, (2048, 64))]
+                 (2, (1024, 0, 0, 1, 4, 0, 2)), (2, (0, 0, 0, 0, 0, 0, 0, 1)), (3, (2048, 64)),
+                 # the prefiltered form (window offset = PAM length for 5' rows)
+                 (2, (0, 0, 0, 0, 0, 1, 0, 0, 1)), (2, (4096, 0, 0, 0, 0, 1, 0, 0, 1)),
+                 (2, (2048, 0, 0, 1, 0, 1, 0, 0, 1))]
         for mode, tune in forms:
             plan.set_tuning(*tune)
             got = f._engine.scan(plan, f._strands, [0, 3], k, mode)
