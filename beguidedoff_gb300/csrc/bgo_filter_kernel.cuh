@@ -67,9 +67,9 @@ struct FiltT {
 // Per-warp shared-memory slice for chunks of CH positions: two chunk buffers
 // (H and L planes, each CH/32 + 4 words; the N plane stays in global memory,
 // read only for survivors of chunks whose N summary is set), the compacted
-// list of PAM-passing
-// positions, the survivor queue (plus one slot that absorbs the stores of
-// lanes without a survivor) and the two chunk buffers' mbarriers.
+// list of the PAM-passing positions' window starts (position + the family's
+// window offset), the survivor queue (plus one slot that absorbs the stores
+// of lanes without a survivor) and the two chunk buffers' mbarriers.
 template <int CH>
 struct FiltChunk {
     static constexpr int kRows = CH / 1024;     // 32-position words per lane
@@ -79,7 +79,11 @@ struct FiltChunk {
     static constexpr int kListCap = CH >= 4096 ? 512 : 1024;
     static constexpr int kPasses = CH / kListCap;
     static constexpr size_t kListOff = 2 * kBuf;
-    static constexpr size_t kQueueOff = kListOff + kListCap * sizeof(uint16_t);
+    // the list array holds whole rounds, so that a round reads entries
+    // without a bound check (entries past the list are valid positions)
+    static constexpr int kListAlloc =
+        (kListCap + 32 * kFilterPer - 1) / (32 * kFilterPer) * (32 * kFilterPer);
+    static constexpr size_t kQueueOff = (kListOff + kListAlloc * sizeof(uint16_t) + 15) / 16 * 16;
     static constexpr size_t kBarOff = kQueueOff + (kSurvCap + 1) * sizeof(uint4);
     static constexpr size_t kSlice = kBarOff + 16;
     static_assert(kPlaneBytes % 16 == 0, "bulk copies are whole 16-byte units");
@@ -261,6 +265,9 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
     const uint32_t buf0 = smem_u32(slice);
 
     if (t == 0) sCand = 0;
+    // every list entry holds a window start inside the chunk buffer, so that
+    // a round may read entries past the list (its lanes keep nothing)
+    for (int i = lane; i < C::kListAlloc; i += 32) wList[i] = 0;
     if (lane == 0) {
         mbar_init(bar0, 1);
         mbar_init(bar0 + 8, 1);
@@ -530,7 +537,7 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                     for (int u = 0; u < C::kRows; ++u) {
                         uint16_t *out = wList + rowoff[u];
                         uint32_t m = pass[u];
-                        const uint32_t wb = 32u * (uint32_t)(u * 32 + lane) + 31u;
+                        const uint32_t wb = 32u * (uint32_t)(u * 32 + lane) + 31u + win_off;
                         // three steps without a loop branch (most words hold at
                         // most three passing positions; the loop after them runs
                         // as long as the warp's fullest word needs), then the
@@ -553,7 +560,7 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                     for (int u = 0; u < C::kRows; ++u) {
                         int off = rowoff[u] - lo;
                         uint32_t m = pass[u];
-                        const uint32_t wb = 32u * (uint32_t)(u * 32 + lane) + 31u;
+                        const uint32_t wb = 32u * (uint32_t)(u * 32 + lane) + 31u + win_off;
                         while (m) {
                             const uint32_t z = __clz(m);
                             m ^= 0x80000000u >> z;
@@ -566,7 +573,8 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                 for (int k0 = 0; k0 < n_list; k0 += 32 * kFilterPer) {
                     // filter: one byte per region key (bit 0: a guide's key
                     // equals it; bits 1-7: colours of the guides within one
-                    // mismatch of it).  Lanes past the list read entry 0 and
+                    // mismatch of it).  Lanes past the list read a stale or
+                    // initial entry (a window start inside the buffer) and
                     // keep nothing.
                     uint32_t sv[kFilterPer], hv[kFilterPer], lv[kFilterPer];
                     bool keep[kFilterPer];
@@ -574,8 +582,8 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                     for (int v = 0; v < kFilterPer; ++v) {
                         const int k = k0 + v * 32 + lane;
                         const bool has = k < n_list;
-                        const uint32_t s = wList[has ? k : 0];
-                        const uint32_t wo = s + win_off;
+                        const uint32_t wo = wList[k];  // the window's start (position + win_off)
+                        const uint32_t s = wo - win_off;
                         const uint32_t wi = wo >> 5, b = wo & 31u;
                         const uint32_t h20 = sfshr(wH[wi], wH[wi + 1], b);
                         const uint32_t l20 = sfshr(wL[wi], wL[wi + 1], b);
@@ -616,7 +624,7 @@ __global__ void __launch_bounds__(kFilterThreads, 1)
                         for (int v = 0; v < kFilterPer; ++v) {
                             const uint32_t s = sv[v];
                             uint32_t n20g = 0;
-                            if (has_n) {
+                            if (has_n && keep[v]) {  // a survivor's s is a listed position
                                 // the chunk's N words, from global memory
                                 const uint32_t *gN =
                                     (strand_bit ? p.strand[1].N : p.strand[0].N) + (base32 >> 5);
