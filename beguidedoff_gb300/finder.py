@@ -440,9 +440,9 @@ class beguidedoff:
                         if not (counts_k.max(axis=1) > limit).any():
                             r0, nr = spans[i]
                             below_by_id: Dict[str, int] = defaultdict(int)
-                            for gid, b in zip(owners[i], below[r0:r0 + nr].tolist()):
-                                below_by_id[gid] += b
-                            hit_keys = np.unique(recs["key"][rec_off[r0]:rec_off[r0 + nr]])
+                            if r["count_score_threshold"] is not None:
+                                for gid, b in zip(owners[i], below[r0:r0 + nr].tolist()):
+                                    below_by_id[gid] += b
                             pre = (limit, below_by_id if r["count_score_threshold"] is not None
                                    else None)
                     if pre is not None and len(self.chrom_names) <= _EXACT_ORDER_CHROMS:
@@ -457,6 +457,9 @@ class beguidedoff:
                         if full is None:
                             _, full = eng.collect(stream)
                         hit_keys = full
+                    else:
+                        r0, nr = spans[i]
+                        hit_keys = np.unique(recs["key"][rec_off[r0]:rec_off[r0 + nr]])
                     out.append(self._assemble(hit_keys, r["keys"], r["key_plan"], plan_items,
                                               r["mapping"], r["guides"], r["return_all"],
                                               r["count_score_threshold"], log, precomputed=pre))
