@@ -41,10 +41,10 @@ UNIT = "cmp/s"
 # form, 4,096-position chunks) of the plain workload at 300 Mbp, from ncu
 # (profiles/scan_filter_kernel_ngg100_300mbp.md); traffic grows with the
 # genome, so the line scales it to the run's length
-NCU_TRAFFIC_PLAIN = (300_000_000, 150.295296e6 + 3.272960e6)
+NCU_TRAFFIC_PLAIN = (300_000_000, 150.274816e6 + 3.204352e6)
 # the same capture's integer-pipe figures: the kernel is issue-bound, so these
 # are its roofline in the integer-ALU sense
-NCU_INT_PLAIN = {"issue_active_frac": 0.780, "alu_pipe_active_frac": 0.683,
+NCU_INT_PLAIN = {"issue_active_frac": 0.776, "alu_pipe_active_frac": 0.686,
                  "warps_active_frac": 0.438,
                  "source": "ncu smsp__issue_active, sm__pipe_alu_cycles_active, "
                            "sm__warps_active (pct of peak, active cycles) at 300 Mbp, "
