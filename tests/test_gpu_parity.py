@@ -286,8 +286,9 @@ def _write_base(genome, ci, p, v, n=False):
 
 @pytest.mark.parametrize("chunk", [2048, 4096])
 def test_prefilter_n_at_chunk_boundaries_equal_oracle(chunk):
-    """The prefiltered form skips the N correction in chunks whose staged N
-    words (the halo included) are all zero.  Sites planted across
+    """The prefiltered form learns whether a chunk or its halo holds an N
+    from the strand's N summary (one bit per 1,024 positions) and reads the N
+    words of its survivors from global memory.  Sites planted across
     1,024-position boundaries of either strand, with a single N inside the
     window at or just past the boundary, so that for a chunk boundary the N
     lies in the previous chunk's halo only (the guide's base there is the
